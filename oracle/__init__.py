@@ -1,0 +1,168 @@
+"""ORACLE — test infrastructure only.
+
+ctypes binding to ``liboracle.so``, the CPU restatement of the reference's
+replica-exchange Wang-Landau path (oracle.cpp, oracle_host.cpp).  Only the
+test-suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
+it, as the checker; the engine never imports it.
+
+``build()`` is the build recipe: one g++ invocation, no external libraries.
+Host float arithmetic is compiled with ``-ffp-contract=off`` so that the
+reference's float expressions (interval.cpp:17-20) round the same way on x86
+and Arm hosts.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SOURCES = ["oracle.cpp", "oracle_host.cpp"]
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    hdr = os.path.join(HERE, "oracle_core.h")
+    if not force and os.path.exists(LIB):
+        newest = max(os.path.getmtime(p) for p in srcs + [hdr])
+        if os.path.getmtime(LIB) >= newest:
+            return LIB
+    cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB + ".tmp", *srcs,
+           "-lpthread"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+        _declare(_lib)
+    return _lib
+
+
+P = C.c_void_p
+i32, u32, i64, u64, f32, f64, sz = C.c_int, C.c_uint, C.c_longlong, C.c_uint64, C.c_float, C.c_double, C.c_size_t
+
+
+def _declare(L):
+    sig = {
+        "orc_philox_raw": (None, [u64, u64, u64, i32, P]),
+        "orc_uniform": (None, [u64, u64, u64, i32, P]),
+        "orc_raw_to_uniform": (f32, [u32]),
+        "orc_interval_results": (i32, [i32, i32, u32, i32, f32, P, P, P, P]),
+        "orc_init_interactions": (None, [P, sz, i32, i32, f32]),
+        "orc_apply_horizontal_error": (None, [P, i32, i32, i32]),
+        "orc_apply_vertical_error": (None, [P, i32, i32, i32]),
+        "orc_apply_error_class": (None, [P, i32, i32, i32, C.c_char]),
+        "orc_init_lattice": (None, [P, i32, i32, sz, i32, i32]),
+        "orc_calc_energy": (None, [i32, P, P, P, P, i32, i32, sz, i32]),
+        "orc_wang_landau_pre_run": (None, [P, P, P, P, P, P, P, P, i32, i32, i32, i32, i32, i32, u32, i32, sz, i32,
+                                           i32]),
+        "orc_wang_landau": (i32, [P] * 17 + [i32] * 8),
+        "orc_check_histogram": (None, [P] * 9 + [f64, i32, i32, i32]),
+        "orc_average_log_g": (None, [P] * 8 + [i32, i32, i32]),
+        "orc_reset_cond": (None, [P, P, i32, f64, i32]),
+        "orc_check_finished": (None, [P, P, i32, i32]),
+        "orc_replica_exchange": (None, [P] * 9 + [i32] * 6),
+        "orc_prerun": (None, [i32, i32, i32, f32, C.c_char, i32, i32, i32, i32, i32, P, P, P, P, P]),
+        "orc_mainrun": (i32, [i32, i32, i32, i32, i32, i32, f32, f64, f64, i32, i32, i32, i32, i32, i64] + [P] * 6
+                        + [i32] + [P] * 8),
+        "orc_stitch": (i32, [P, P, P, i32, i32, i32, i32, P, P, i32, P]),
+        "orc_exact_counts": (None, [P, i32, i32, i32, P]),
+        "orc_enumerate_counts": (None, [P, i32, i32, i32, P]),
+        "orc_log_partition": (f64, [P, P, i32, f64]),
+        "orc_run_problems": (i64, [P, i32, i32, P, P, P]),
+        "orc_exp_log": (None, [P, P, P, i32]),
+        "orc_sqrt_chain": (None, [f64, i32, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def ptr(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ----------------------------------------------------------------- wrappers --
+
+def uniforms(key: int, subseq: int, offset: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    lib().orc_uniform(key, subseq, offset, n, ptr(out))
+    return out
+
+
+def philox_raw(key: int, subseq: int, offset: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().orc_philox_raw(key, subseq, offset, n, ptr(out))
+    return out
+
+
+def interval_results(e_min, e_max, n_int, walkers, overlap):
+    """interval.cpp:5-41 -> (start, end, len_hist_all, len_interval); raises ValueError like the reference."""
+    s = np.zeros(n_int, np.int32)
+    e = np.zeros(n_int, np.int32)
+    tot = C.c_longlong(0)
+    ln = C.c_int(0)
+    rc = lib().orc_interval_results(e_min, e_max, n_int, walkers, C.c_float(overlap), ptr(s), ptr(e),
+                                    C.byref(tot), C.byref(ln))
+    if rc == 1:
+        raise ValueError("Overlap is out of bounds.")
+    if rc == 2:
+        raise ValueError("The interval arguments create empty intervals.")
+    return s, e, tot.value, ln.value
+
+
+def init_interactions(X, Y, R, seed, prob, cls="i"):
+    J = np.zeros(R * 2 * X * Y, np.int8)
+    lib().orc_init_interactions(ptr(J), X * Y, R, seed, C.c_float(prob))
+    lib().orc_apply_error_class(ptr(J), X, Y, R, cls.encode())
+    return J
+
+
+def init_lattice(X, Y, num_lattices, seed, wpi):
+    lat = np.zeros(num_lattices * X * Y, np.int8)
+    lib().orc_init_lattice(ptr(lat), X, Y, num_lattices, seed, wpi)
+    return lat
+
+
+def calc_energy(boundary, lat, J, off_lat, X, Y, num_lattices, wpi):
+    E = np.zeros(num_lattices, np.int32)
+    lib().orc_calc_energy(boundary, ptr(E), ptr(lat), ptr(J), ptr(off_lat), X, Y, num_lattices, wpi)
+    return E
+
+
+def exact_counts(J, X, Y, boundary, brute=False):
+    c = np.zeros(4 * X * Y + 1, np.float64)
+    fn = lib().orc_enumerate_counts if brute else lib().orc_exact_counts
+    fn(ptr(np.ascontiguousarray(J, np.int8)), X, Y, boundary, ptr(c))
+    return c
+
+
+class OrcProblem(C.Structure):
+    _fields_ = [("X", i32), ("Y", i32), ("boundary", i32), ("prob", f32), ("error_class", i32), ("seed", i32),
+                ("sample", i32), ("pre_walkers", i32), ("pre_intervals", i32), ("pre_iterations", i32),
+                ("n_int", i32), ("W", i32), ("overlap", f32), ("alpha", f64), ("beta", f64), ("n_iter", i32),
+                ("exchange_every", i32), ("exchange_mode", i32), ("max_outer", i64)]
+
+
+def run_problems(problems, threads):
+    """Whole problems (pre-run + main run) on host threads; returns (status, outer, flips)."""
+    n = len(problems)
+    arr = (OrcProblem * n)(*problems)
+    st = np.zeros(n, np.int32)
+    outer = np.zeros(n, np.int64)
+    fl = np.zeros(n, np.int64)
+    lib().orc_run_problems(C.cast(arr, C.c_void_p), n, threads, ptr(st), ptr(outer), ptr(fl))
+    return st, outer, fl

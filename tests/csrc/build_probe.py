@@ -1,0 +1,16 @@
+"""Builds the test-only cuRAND probe library (tests/csrc/libprobe.so)."""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libprobe.so")
+
+
+def build() -> str:
+    src = os.path.join(HERE, "curand_probe.cu")
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    subprocess.run(["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC",
+                    "-shared", "-o", LIB + ".tmp", src], check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB

@@ -1,0 +1,60 @@
+// Test-only probe: draws from cuRAND's Philox4_32_10 device API and CUDA's
+// double exp/log, so the tests can pin the engine's own Philox streams and
+// the oracle's host arithmetic against what the reference's kernels compute.
+#include <cstdint>
+#include <curand_kernel.h>
+
+namespace {
+
+__global__ void k_curand(const unsigned long long* seeds, const unsigned long long* subseqs,
+                         const unsigned long long* offsets, int n_triples, int n_draws, float* out)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n_triples) return;
+  curandStatePhilox4_32_10_t st;
+  curand_init(seeds[q], subseqs[q], offsets[q], &st);
+  for (int d = 0; d < n_draws; ++d) out[static_cast<size_t>(q) * n_draws + d] = curand_uniform(&st);
+}
+
+__global__ void k_exp_log(const double* x, double* e, double* l, int n)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  e[q] = exp(x[q]);
+  l[q] = log(x[q]);
+}
+
+__global__ void k_sqrt_chain(double x0, int n, double* f, double* lf)
+{
+  double x = x0;
+  for (int q = 0; q < n; ++q) {
+    f[q] = x;
+    lf[q] = log(x);
+    x = sqrt(x);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int probe_curand_uniform(const unsigned long long* d_seeds, const unsigned long long* d_subseqs,
+                         const unsigned long long* d_offsets, int n_triples, int n_draws, float* d_out)
+{
+  k_curand<<<(n_triples + 127) / 128, 128>>>(d_seeds, d_subseqs, d_offsets, n_triples, n_draws, d_out);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
+int probe_exp_log(const double* d_x, double* d_exp, double* d_log, int n)
+{
+  k_exp_log<<<(n + 127) / 128, 128>>>(d_x, d_exp, d_log, n);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
+int probe_sqrt_chain(double x0, int n, double* d_f, double* d_logf)
+{
+  k_sqrt_chain<<<1, 1>>>(x0, n, d_f, d_logf);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
+}  // extern "C"

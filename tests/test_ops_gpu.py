@@ -1,0 +1,336 @@
+"""GPU parity of the operator layer (reference layout) against the oracle.
+
+Integer outputs (couplings, lattices, energies, histograms, flags, RNG
+offsets, exchange decisions) must be bit-exact; log g too, because both
+sides perform the same FP64 operations in the same order.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle as O
+from tests.helpers import (Dev, assert_state_equal, copy_state, mainrun_state, o_average, o_check_histogram,
+                           o_exchange, o_reset_finish, o_wang_landau, prerun_outputs)
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def probe(cuda):
+    sys.path.insert(0, os.path.join(HERE, "csrc"))
+    import build_probe
+    L = C.CDLL(build_probe.build())
+    for n in ("probe_curand_uniform", "probe_exp_log", "probe_sqrt_chain"):
+        getattr(L, n).restype = C.c_int
+    L.probe_sqrt_chain.argtypes = [C.c_double, C.c_int, C.c_void_p, C.c_void_p]
+    return L
+
+
+def _dptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+TRIPLES = [(0, 0, 0), (1, 0, 0), (12345, 0, 5), (12345, 3, 0), (12345, 3, 1), (12345, 3, 2), (12345, 3, 3),
+           (12345, 29, 1001), (2 ** 32 + 7, 2, 77), ((-5) % 2 ** 64, 1, 13), (4294967291, 127, 2 ** 33 + 3),
+           (987654321, 2 ** 40 + 5, 3), (42, 0, 123456789), (7, 1, 31)]
+
+
+def test_philox_streams_match_curand(cuda, probe):
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    n_draws = 37
+    seeds = torch.tensor(np.array([t[0] for t in TRIPLES], np.uint64).view(np.int64)).cuda()
+    subs = torch.tensor(np.array([t[1] for t in TRIPLES], np.uint64).view(np.int64)).cuda()
+    offs = torch.tensor(np.array([t[2] for t in TRIPLES], np.uint64).view(np.int64)).cuda()
+    ref = torch.zeros(len(TRIPLES) * n_draws, dtype=torch.float32, device="cuda")
+    assert probe.probe_curand_uniform(_dptr(seeds), _dptr(subs), _dptr(offs), len(TRIPLES), n_draws, _dptr(ref)) == 0
+    ref = ref.cpu().numpy().reshape(len(TRIPLES), n_draws)
+    mine = torch.zeros(n_draws, dtype=torch.float32, device="cuda")
+    for q, (k, s, o) in enumerate(TRIPLES):
+        wlg.call("wlg_uniforms", k, s, o, n_draws, _dptr(mine), None)
+        torch.cuda.synchronize()
+        got = mine.cpu().numpy()
+        host = O.uniforms(k, s, o, n_draws)
+        assert np.array_equal(got.view(np.uint32), ref[q].view(np.uint32)), f"engine vs cuRAND, triple {q}"
+        assert np.array_equal(host.view(np.uint32), ref[q].view(np.uint32)), f"oracle vs cuRAND, triple {q}"
+
+
+def test_device_log_of_factor_chain_matches_host(cuda, probe):
+    """ln f of every modification factor e, e^(1/2), e^(1/4), ... is bit-identical on host and device."""
+    torch = cuda
+    n = 60
+    f = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lf = torch.zeros(n, dtype=torch.float64, device="cuda")
+    assert probe.probe_sqrt_chain(np.e, n, _dptr(f), _dptr(lf)) == 0
+    hf = np.zeros(n)
+    hlf = np.zeros(n)
+    O.lib().orc_sqrt_chain(np.e, n, O.ptr(hf), O.ptr(hlf))
+    assert np.array_equal(f.cpu().numpy(), hf)
+    assert np.array_equal(lf.cpu().numpy(), hlf)
+
+
+def test_prerun_acceptance_exp_decisions_match(cuda, probe):
+    """exp(H_old - H_new) of integer count differences: every float uniform
+    compares the same way against the device and host values."""
+    torch = cuda
+    x = np.arange(-1100, 1101, dtype=np.float64)
+    dx = torch.from_numpy(x).cuda()
+    de = torch.zeros_like(dx)
+    dl = torch.zeros_like(dx)
+    assert probe.probe_exp_log(_dptr(dx), _dptr(de), _dptr(dl), len(x)) == 0
+    he = np.zeros_like(x)
+    hl = np.zeros_like(x)
+    O.lib().orc_exp_log(O.ptr(np.ascontiguousarray(x)), O.ptr(he), O.ptr(hl), len(x))
+    ge = de.cpu().numpy()
+    for a, b in zip(ge, he):
+        lo, hi = min(a, b), max(a, b)
+        if lo == hi or hi <= 0:
+            continue
+        # no float strictly inside [lo, hi) may separate the decisions
+        f = np.float32(lo)
+        f = f if f >= lo else np.nextafter(f, np.float32(np.inf))
+        assert not (lo <= float(f) < hi), (a, b)
+
+
+@pytest.mark.parametrize("X,Y,R,seed,prob", [(4, 4, 3, 1, 0.15), (6, 6, 5, 12345, 0.04), (7, 5, 4, -17, 0.5),
+                                             (24, 24, 2, 99, 0.1), (3, 9, 6, 2 ** 31 - 3, 0.3)])
+@pytest.mark.parametrize("cls", ["i", "h", "v", "c"])
+def test_init_interactions(cuda, X, Y, R, seed, prob, cls):
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    d = torch.zeros(R * 2 * X * Y, dtype=torch.int8, device="cuda")
+    wlg.call("wlg_init_interactions", _dptr(d), X * Y, R, seed, C.c_float(prob), None)
+    wlg.call("wlg_apply_error_class", _dptr(d), X, Y, R, cls.encode(), None)
+    ref = O.init_interactions(X, Y, R, seed, prob, cls)
+    assert np.array_equal(d.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("X,Y,nl,seed,wpi", [(4, 4, 10, 5, 5), (6, 6, 12, 12345, 4), (5, 7, 9, -3, 3),
+                                             (24, 24, 4, 1, 2)])
+def test_init_lattice(cuda, X, Y, nl, seed, wpi):
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    d = torch.zeros(nl * X * Y, dtype=torch.int8, device="cuda")
+    wlg.call("wlg_init_lattice", _dptr(d), X, Y, nl, seed, wpi, None)
+    assert np.array_equal(d.cpu().numpy(), O.init_lattice(X, Y, nl, seed, wpi))
+
+
+@pytest.mark.parametrize("boundary", [0, 1])
+@pytest.mark.parametrize("X,Y", [(4, 4), (6, 6), (5, 3), (16, 16), (24, 24)])
+def test_calc_energy(cuda, boundary, X, Y):
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    rng = np.random.default_rng(X * 100 + Y + boundary)
+    R, wpi = 3, 4
+    nl = R * wpi
+    lat = rng.choice(np.array([-1, 1], np.int8), nl * X * Y)
+    J = rng.choice(np.array([-1, 1], np.int8), R * 2 * X * Y)
+    off = (np.arange(nl) * X * Y).astype(np.int32)
+    dl, dJ, do = (torch.from_numpy(a).cuda() for a in (lat, J, off))
+    dE = torch.zeros(nl, dtype=torch.int32, device="cuda")
+    wlg.call("wlg_calc_energy", boundary, _dptr(dE), _dptr(dl), _dptr(dJ), _dptr(do), X, Y, nl, wpi, None)
+    assert np.array_equal(dE.cpu().numpy(), O.calc_energy(boundary, lat, J, off, X, Y, nl, wpi))
+
+
+def test_calc_energy_known_answers(cuda):
+    """test_calc_energy.cu: -6 periodic / -4 open for the literal 4x4 case; all-up lattices."""
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    lat = np.array([1, 1, -1, 1, -1, -1, 1, -1, 1, -1, 1, -1, -1, -1, -1, -1], np.int8)
+    J = np.array([1, -1, 1, 1, 1, 1, 1, 1, -1, 1, 1, -1, 1, 1, 1, 1, 1, 1, -1, 1, 1, 1, 1, 1, -1, 1, 1, 1, 1, 1, 1,
+                  1], np.int8)
+    for boundary, want in ((0, -6), (1, -4)):
+        dE = torch.zeros(1, dtype=torch.int32, device="cuda")
+        wlg.call("wlg_calc_energy", boundary, _dptr(dE), _dptr(torch.from_numpy(lat).cuda()),
+                 _dptr(torch.from_numpy(J).cuda()), _dptr(torch.zeros(1, dtype=torch.int32, device="cuda")), 4, 4, 1,
+                 1, None)
+        assert int(dE.item()) == want
+    ones = torch.ones(10 * 16, dtype=torch.int8, device="cuda")
+    Jones = torch.ones(2 * 32, dtype=torch.int8, device="cuda")
+    off = torch.arange(10, dtype=torch.int32, device="cuda") * 16
+    for boundary, want in ((0, -32), (1, -32 + 8)):
+        dE = torch.zeros(10, dtype=torch.int32, device="cuda")
+        wlg.call("wlg_calc_energy", boundary, _dptr(dE), _dptr(ones), _dptr(Jones), _dptr(off), 4, 4, 10, 5, None)
+        assert (dE.cpu().numpy() == want).all()
+
+
+@pytest.mark.parametrize("X,Y,boundary,R,wpi,n_int,n_iter,seed,prob", [
+    (4, 4, 0, 2, 32, 8, 500, 12345, 0.04),
+    (4, 4, 1, 2, 16, 5, 300, 7, 0.0),
+    (6, 6, 0, 3, 128, 32, 200, 12345, 0.04),
+    (5, 7, 1, 2, 40, 9, 150, -11, 0.2),
+])
+def test_prerun_walk(cuda, X, Y, boundary, R, wpi, n_int, n_iter, seed, prob):
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    N = X * Y
+    J = O.init_interactions(X, Y, R, seed, prob, "v")
+    T = R * wpi
+    lat = O.init_lattice(X, Y, T, seed, wpi)
+    off = (np.arange(T) * N).astype(np.int32)
+    E = O.calc_energy(boundary, lat, J, off, X, Y, T, wpi)
+    s, e, _, len_int = O.interval_results(-2 * N, 2 * N, n_int, 1, 1.0)
+    L = 4 * N + 1
+    H = np.zeros(R * L, np.uint64)
+    flags = np.zeros(R * n_int, np.int32)
+    flat = np.zeros(R * n_int * N, np.int8)
+    so = np.zeros(T, np.uint64)
+    dev = {k: torch.from_numpy(v.view(np.int64) if v.dtype == np.uint64 else v.copy()).cuda()
+           for k, v in dict(E=E, flags=flags, lat=lat, flat=flat, H=H, so=so, J=J, off=off).items()}
+    wlg.call("wlg_wang_landau_pre_run", _dptr(dev["E"]), _dptr(dev["flags"]), _dptr(dev["lat"]), _dptr(dev["flat"]),
+             _dptr(dev["H"]), _dptr(dev["so"]), _dptr(dev["J"]), _dptr(dev["off"]), -2 * N, 2 * N, n_iter, X, Y,
+             seed, n_int, len_int, T, wpi, boundary, None)
+    p = O.ptr
+    O.lib().orc_wang_landau_pre_run(p(E), p(flags), p(lat), p(flat), p(H), p(so), p(J), p(off), -2 * N, 2 * N, n_iter,
+                                    X, Y, seed, n_int, len_int, T, wpi, boundary)
+    torch.cuda.synchronize()
+    assert np.array_equal(dev["E"].cpu().numpy(), E)
+    assert np.array_equal(dev["lat"].cpu().numpy(), lat)
+    assert np.array_equal(dev["H"].cpu().numpy().view(np.uint64), H)
+    assert np.array_equal(dev["flags"].cpu().numpy(), flags)
+    assert np.array_equal(dev["flat"].cpu().numpy(), flat)
+    assert np.array_equal(dev["so"].cpu().numpy().view(np.uint64), so)
+    assert (so == 2 * n_iter).all()
+
+
+CASES = [
+    # X, Y, boundary, R, I, W, overlap, cls, seed, prob, n_iter, iters, exchange_every
+    (4, 4, 0, 2, 4, 3, 0.25, "i", 12345, 0.04, 200, 40, 1),
+    (4, 4, 1, 2, 3, 4, 0.3, "c", 99, 0.1, 150, 30, 2),
+    (6, 6, 0, 3, 10, 3, 0.25, "v", 12345, 0.04, 300, 25, 3),
+    (5, 4, 1, 2, 5, 2, 0.5, "h", -21, 0.2, 100, 30, 1),
+]
+
+
+@pytest.mark.parametrize("X,Y,boundary,R,I,W,overlap,cls,seed,prob,n_iter,iters,xc", CASES)
+def test_mainrun_operators_step_by_step(cuda, X, Y, boundary, R, I, W, overlap, cls, seed, prob, n_iter, iters, xc):
+    """The reference's outer loop (mainrun.cu:243-374) driven through the
+    operators on GPU and on the oracle; every array equal after every step."""
+    torch = cuda
+    pre = prerun_outputs(X, Y, boundary, prob, cls, seed, R, 32, 12, 2000)
+    st = mainrun_state(pre, I, W, overlap)
+    dev = Dev(torch, copy_state(st))
+    alpha, beta = 0.8, 0.05
+    for it in range(iters):
+        n_new = o_wang_landau(st, n_iter, seed)
+        dev.wang_landau(n_iter, seed)
+        assert_state_equal(dev.snapshot(), st, f"iter {it} wang_landau")
+        assert n_new == 0
+        o_check_histogram(st, alpha)
+        dev.check_histogram(alpha)
+        o_average(st)
+        dev.average()
+        o_reset_finish(st, beta)
+        dev.reset_finish(beta)
+        assert_state_equal(dev.snapshot(), st, f"iter {it} flatness")
+        if (it + 1) % xc == 0:
+            for even in (1, 0):
+                o_exchange(st, even, seed, global_parity=it % 2)
+                dev.exchange(even, seed, global_parity=it % 2)
+            assert_state_equal(dev.snapshot(), st, f"iter {it} exchange")
+    # the run made progress: some windows went flat at least once
+    assert (st["factor"] < np.e).any()
+
+
+def test_new_energy_flags(cuda):
+    torch = cuda
+    pre = prerun_outputs(4, 4, 0, 0.04, "i", 3, 2, 32, 8, 2000)
+    st = mainrun_state(pre, 3, 2, 0.25)
+    # punch a hole into sample 1's spectrum at a reachable energy
+    k = 1
+    lo = st["off_spec"][k]
+    hole = lo + 2 * 4 if st["spectrum"][lo + 8] == 1 else lo + 4 * 3
+    st["spectrum"][hole] = 0
+    dev = Dev(torch, copy_state(st))
+    for _ in range(20):
+        o_wang_landau(st, 500, 3)
+        dev.wang_landau(500, 3)
+    assert_state_equal(dev.snapshot(), st, "new energy")
+    assert (st["found"][:6] == 0).all()
+    assert (st["found"][6:] != 0).any()
+
+
+def test_check_histogram_reference_vector(cuda):
+    """test_check_histogram.cu:23-126 on the GPU."""
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    H = np.full(80, 10, np.uint64)
+    H[0] = 1
+    start = np.array([-2, -1, 0, -4, -2, 0, -2, -1, 0], np.int32)
+    end = np.array([-1, 0, 2, -2, 0, 2, -2, -1, 1], np.int32)
+    cond_inter = np.array([1, 1, 1], np.int32)
+    off_hist = np.array([0, 2, 4, 6, 8, 10, 12, 14] + [16 + 3 * q for q in range(16)] + [64 + q for q in range(8)]
+                        + [72, 74, 76, 78], np.int32)
+    cond = np.array([0, 0, 0, 0, 0, 0, 0, 0, 1], np.int8)
+    off_spec = np.array([0, 7, 16], np.int32)
+    spec = np.ones(20, np.int8)
+    factor = np.full(36, np.e)
+    d = {k: torch.from_numpy(v.view(np.int64) if v.dtype == np.uint64 else v.copy()).cuda()
+         for k, v in dict(H=H, factor=factor, cond=cond, off_hist=off_hist, end=end, start=start, spec=spec,
+                          off_spec=off_spec, ci=cond_inter).items()}
+    wlg.call("wlg_check_histogram", _dptr(d["H"]), _dptr(d["factor"]), _dptr(d["cond"]), _dptr(d["off_hist"]),
+             _dptr(d["end"]), _dptr(d["start"]), _dptr(d["spec"]), _dptr(d["off_spec"]), _dptr(d["ci"]), 0.8, 36, 12,
+             3, None)
+    torch.cuda.synchronize()
+    want_H = np.zeros(80, np.uint64)
+    want_H[:8] = 10
+    want_H[72:] = 10
+    want_H[0] = 1
+    assert np.array_equal(d["H"].cpu().numpy().view(np.uint64), want_H)
+    assert d["cond"].cpu().numpy().tolist() == [0, 1, 1, 1, 1, 1, 1, 1, 1]
+    want_f = np.full(36, np.sqrt(np.e))
+    want_f[:4] = np.e
+    want_f[32:] = np.e
+    assert np.allclose(d["factor"].cpu().numpy(), want_f, rtol=1e-15, atol=0)
+
+
+def test_replica_exchange_flat_log_g_swaps_by_permutation(cuda):
+    """test_replica_exchange.cu:36-158: with flat log g every admissible pair swaps."""
+    torch = cuda
+    R, I, W = 3, 10, 5
+    T = R * I * W
+    start = np.zeros(R * I, np.int32)
+    end = np.zeros(R * I, np.int32)
+    E = np.zeros(T, np.int32)
+    off_hist = np.zeros(T, np.int32)
+    off_lat = np.zeros(T, np.int32)
+    acc = 0
+    for b in range(R * I):
+        bl, k = b % I, b // I
+        start[b], end[b] = bl + k, bl + k + 4
+        for w in range(W):
+            t = b * W + w
+            E[t] = bl + k + 2
+            off_hist[t] = acc
+            acc += 5
+            off_lat[t] = t * 9
+    st = dict(R=R, I=I, W=W, start=start, end=end, E=E, off_hist=off_hist, off_lat=off_lat,
+              logG=np.ones(acc), perm=(np.arange(T) % W).astype(np.int32), off_iter=np.zeros(T, np.uint64),
+              cond_inter=np.ones(R, np.int32))
+    ref = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
+    o_exchange(ref, 1, 42, global_parity=1)
+    import qec_pf_wang_landau_gb300 as wlg
+    d = {k: torch.from_numpy(v.view(np.int64) if v.dtype == np.uint64 else v.copy()).cuda() for k, v in st.items()
+         if isinstance(v, np.ndarray)}
+    wlg.call("wlg_replica_exchange", _dptr(d["off_lat"]), _dptr(d["E"]), _dptr(d["perm"]), _dptr(d["off_iter"]),
+             _dptr(d["start"]), _dptr(d["end"]), _dptr(d["off_hist"]), _dptr(d["cond_inter"]), _dptr(d["logG"]), 1, 42,
+             I, I * W, R * I, 1, None)
+    torch.cuda.synchronize()
+    got_off = d["off_lat"].cpu().numpy()
+    perm = d["perm"].cpu().numpy()
+    assert np.array_equal(got_off, ref["off_lat"])
+    assert np.array_equal(perm, ref["perm"])
+    assert np.array_equal(d["off_iter"].cpu().numpy().view(np.uint64), ref["off_iter"])
+    for b in range(R * I):
+        if b % I == I - 1 or b % 2:
+            continue
+        assert sorted(perm[b * W:(b + 1) * W].tolist()) == list(range(W))
+        for w in range(W):
+            t = b * W + w
+            o = (b + 1) * W + perm[t]
+            assert got_off[t] == off_lat[o] and got_off[o] == off_lat[t]
