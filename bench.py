@@ -1,0 +1,292 @@
+"""Benchmark: converged disorder samples per second (and WL flips per second)
+of the batched GB300 engine on the reference's matched workload.
+
+Workload (one "step"): 6x6 periodic random-bond Ising lattices, bond flip
+probability 0.04, 100 disorder samples x error classes i/v/h/c = 400
+problems, seed 12345; pre-run 128 walkers, 32 coarse bins, 1000 iterations;
+main run 10 windows x 3 walkers, overlap 0.25, flatness 0.8, final ln f
+1e-3, 1000 WL steps per check, replica exchange every 20 checks.  Every
+problem runs pre-run + main run to convergence.
+
+value  = converged problems / (pre-run kernel + host hand-off + main-run
+         kernel time), the kernels timed with CUDA events;
+e2e    = the same through wlg_solve() with host buffers: problem
+         descriptors in, stitched log g out, everything in the timed region;
+--impl reference times the CPU restatement of the reference's path (the
+reference has no CPU implementation and its CUDA build needs Boost/HDF5) on
+all host cores.
+
+Multi-GPU (torchrun): the problems shard by disorder sample, one shard of
+400 problems per rank (weak scaling), no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(X=6, Y=6, boundary=0, prob=0.04, seed=12345, samples=100, classes="ivhc", pre_walkers=128,
+                pre_intervals=32, pre_iterations=1000, intervals=10, walkers_per_interval=3, overlap=0.25, alpha=0.8,
+                beta=1e-3, iterations=1000, exchange_every=20)
+BYTES_PER_FLIP = 34  # log g read old + read new + write (24 B), histogram RMW (8 B), packed neighbourhood (~2 B)
+METRIC = "disorder samples converged/s (6x6 periodic p=0.04, 100 samples x 4 classes)"
+CPU_SAMPLE_PROBLEMS = 96
+
+
+def problems(rank: int = 0):
+    import qec_pf_wang_landau_gb300 as wlg
+    w = WORKLOAD
+    out = []
+    for k in range(w["samples"]):
+        for c in w["classes"]:
+            out.append(wlg.problem(w["X"], w["Y"], boundary=w["boundary"], prob=w["prob"], error_class=c,
+                                   seed=w["seed"], sample=rank * w["samples"] + k, pre_walkers=w["pre_walkers"],
+                                   pre_intervals=w["pre_intervals"], pre_iterations=w["pre_iterations"],
+                                   intervals=w["intervals"], walkers_per_interval=w["walkers_per_interval"],
+                                   overlap=w["overlap"], alpha=w["alpha"], beta=w["beta"],
+                                   iterations=w["iterations"], exchange_every=w["exchange_every"], exchange_mode=1))
+    return out
+
+
+def cpu_problems(n: int):
+    import oracle as O
+    w = WORKLOAD
+    out = []
+    for q in range(n):
+        k, c = divmod(q, len(w["classes"]))
+        out.append(O.OrcProblem(w["X"], w["Y"], w["boundary"], w["prob"], ord(w["classes"][c]), w["seed"], k,
+                                w["pre_walkers"], w["pre_intervals"], w["pre_iterations"], w["intervals"],
+                                w["walkers_per_interval"], w["overlap"], w["alpha"], w["beta"], w["iterations"],
+                                w["exchange_every"], 1, 0))
+    return out
+
+
+def cpu_run(n: int, threads: int):
+    """The oracle's C++ restatement on `threads` host threads: (problems/s, flips/s, seconds)."""
+    import oracle as O
+    probs = cpu_problems(n)
+    t0 = time.perf_counter()
+    st, outer, fl = O.run_problems(probs, threads)
+    dt = time.perf_counter() - t0
+    ok = int((st == 0).sum())
+    return ok / dt, float(fl.sum()) / dt, dt
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self, device_index: int = 0):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(device_index):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.remove(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(torch, buf):
+    buf.add_(1)  # 512 MiB read+write, far beyond the 129 MB L2
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    import torch
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, dist
+
+
+def run_ours(args):
+    import torch
+    import qec_pf_wang_landau_gb300 as wlg
+    wlg.build()
+    rank, ws, dist = dist_init()
+    dev = torch.cuda.current_device()
+    ctx = wlg.Context(dev)
+    probs = problems(rank)
+    flush = torch.zeros(128 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        ctx.solve(probs)
+    torch.cuda.synchronize()
+    sampler = ClockSampler()
+    if rank == 0:
+        sampler.start()
+    dev_ms, e2e_s, converged, flips, main_ms = [], [], 0, 0, []
+    h2d = d2h = launches = 0
+    for _ in range(args.steps):
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        out = ctx.solve(probs)  # wlg_solve synchronises its own stream before returning
+        e2e_s.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        dev_ms.append(st["pre_ms"] + st["handoff_ms"] + st["main_ms"])
+        main_ms.append(st["main_ms"])
+        converged += sum(1 for r, _, _ in out if r.status == 0)
+        flips += sum(r.flips for r, _, _ in out)
+        h2d, d2h, launches = st["h2d_bytes"], st["d2h_bytes"], launches + st["kernel_launches"]
+    torch.cuda.synchronize()
+    clocks = sampler.stop(dev) if rank == 0 else None
+    t_dev = sum(dev_ms) / 1e3
+    t_e2e = sum(e2e_s)
+    t_main = sum(main_ms) / 1e3
+    if dist is not None:
+        tt = torch.tensor([t_dev, t_e2e, t_main], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev, t_e2e, t_main = tt.tolist()
+        cc = torch.tensor([converged, flips], dtype=torch.float64, device="cuda")
+        dist.all_reduce(cc, op=dist.ReduceOp.SUM)
+        converged, flips = int(cc[0].item()), int(cc[1].item())
+    if rank != 0:
+        return None
+    peaks, peak_kind = measured_peaks()
+    achieved = BYTES_PER_FLIP * flips / max(t_main, 1e-12) / 1e9
+    cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1)
+    line = {
+        "metric": METRIC,
+        "value": converged / t_dev,
+        "unit": "samples/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32+f64",
+        "data": "synthetic: seeded Philox disorder (reference streams), no dataset",
+        "config": {"workload": "6x6 periodic, p=0.04, 100 disorder samples x classes ivhc, prerun 128w/32i/1000n, "
+                               "mainrun 10 windows x 3 walkers, o=0.25, alpha=0.8, ln f 1e-3, n=1000, exchange every 20",
+                   "problems_per_gpu": len(probs), "l2": "flushed between steps (512 MiB write)"},
+        "flips_per_s": flips / t_main,
+        "converged": converged,
+        "e2e": {"value": converged / t_e2e, "unit": "samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
+                     "basis": f"{BYTES_PER_FLIP} algorithmic B per WL flip of the main-run kernel"},
+        "cpu_baseline": {"value": cpu_pps, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
+                         "flips_per_s": cpu_fps,
+                         "sample": f"{CPU_SAMPLE_PROBLEMS} problems of the same workload (samples 0-23 x ivhc), "
+                                   f"{cpu_s:.1f} s wall"},
+    }
+    if clocks is not None:
+        line["clocks"] = clocks
+    return line
+
+
+def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's path (oracle
+    port) on every host thread, same workload, bounded sample per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_run(threads, threads)
+    tot_p, tot_s, tot_f = 0.0, 0.0, 0.0
+    for _ in range(args.steps):
+        pps, fps, dt = cpu_run(CPU_SAMPLE_PROBLEMS, threads)
+        tot_p += pps * dt
+        tot_f += fps * dt
+        tot_s += dt
+    v = tot_p / tot_s
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": "samples/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot_s / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32+f64",
+        "data": "synthetic: seeded Philox disorder (reference streams), no dataset",
+        "config": {"workload": "6x6 periodic, p=0.04, classes ivhc, same flags as the GPU arm",
+                   "problems_per_step": CPU_SAMPLE_PROBLEMS},
+        "flips_per_s": tot_f / tot_s,
+        "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
+                         "sample": f"{CPU_SAMPLE_PROBLEMS} problems per step on {threads} threads (the reference "
+                                   f"has no CPU path; its CUDA build needs Boost and HDF5)"},
+        "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

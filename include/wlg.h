@@ -151,6 +151,97 @@ wlg_status wlg_max_f64_nonneg(const double* d_in, size_t n, double* d_out, wlg_s
  * followed by curand_uniform would give. */
 wlg_status wlg_uniforms(uint64_t key, uint64_t subseq, uint64_t offset, int n, float* d_out, wlg_stream stream);
 
+/* ===================================================================== *
+ *  2. Engine (context-owned device memory)                               *
+ * ===================================================================== */
+
+/* One Wang-Landau problem: disorder sample `sample` of a run seeded `seed`,
+ * one error class.  The reference's `prerun -x X -y Y -p prob -n
+ * pre_iterations -w pre_walkers -i pre_intervals -e class -r R -s seed`
+ * followed by `mainrun -n iterations -a alpha -b beta -i intervals -w
+ * walkers_per_interval -o overlap -c exchange_every ...` computes problems
+ * sample = 0..R-1 (prerun.cu, mainrun.cu); every problem here reproduces the
+ * reference's Philox streams for its (seed, sample). */
+typedef struct {
+  int X, Y;
+  int boundary;           /* 0 periodic, 1 open */
+  float prob;             /* bond flip probability (-p) */
+  char error_class;       /* 'i' (or 'I'), 'h', 'v', 'c' (-e) */
+  int seed;               /* run seed (-s); pre-run and main run use the same one */
+  int sample;             /* disorder sample index within the run */
+  int pre_walkers;        /* prerun -w, <= 1024 */
+  int pre_intervals;      /* prerun -i */
+  int pre_iterations;     /* prerun -n */
+  int intervals;          /* mainrun -i */
+  int walkers_per_interval; /* mainrun -w */
+  float overlap;          /* mainrun -o */
+  double alpha;           /* mainrun -a, flatness */
+  double beta;            /* mainrun -b, final ln f */
+  int iterations;         /* mainrun -n, WL steps per walker between flatness checks */
+  int exchange_every;     /* mainrun -c */
+  int exchange_mode;      /* 0: as the reference (its counter never advances, so exchange runs
+                             only when exchange_every == 1); 1: every exchange_every iterations */
+  int global_parity;      /* 1: exchange parity on the run-global window index (sample*intervals + b),
+                             as the reference; 0: on the window index inside the problem */
+  long long max_outer;    /* cap on outer iterations, 0 = none (the reference's --time_limit analogue) */
+} wlg_problem;
+
+typedef struct {
+  int status;             /* WLG_OK, WLG_ERR_NEW_ENERGY, WLG_ERR_TIMEOUT, WLG_ERR_NO_LATTICE, ... */
+  int new_energy;         /* the offending energy when status == WLG_ERR_NEW_ENERGY */
+  long long outer_iterations;
+  long long flips;        /* WL move attempts of the main run */
+  long long pre_flips;    /* move attempts of the pre-run */
+  int n_energies;         /* (E, log g) pairs of the stitched, normalised result */
+  long long offset;       /* where they start in the caller's arrays */
+} wlg_result;
+
+typedef struct wlg_context wlg_context;
+
+/* A context owns a CUDA stream and the device buffers of the engine on
+ * `device`.  mem_budget_bytes = 0 means no limit beyond the device's. */
+wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context** out);
+wlg_status wlg_context_destroy(wlg_context* ctx);
+const char* wlg_context_last_error(const wlg_context* ctx);
+
+/* Runs pre-run and main run of n problems as one batch on the GPU and
+ * returns each problem's stitched, normalised log g (result_handling.cpp,
+ * logsumexp = X*Y*ln 2): pairs (energies[i], log_g[i]) for i in
+ * [offset, offset + n_energies).  capacity bounds the pair arrays
+ * (4*X*Y + 1 per problem always suffices).  Per-problem failures are in
+ * results[].status; the call itself fails only on invalid input or a
+ * device error. */
+wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* energies,
+                     double* log_g, long long capacity);
+
+/* Like wlg_solve, without stitching: the walker-0 log g of every window on
+ * the reference's dense per-window layout (window b covers energies
+ * win_start..win_end, zeros at unreachable energies), problem after
+ * problem, window after window.  win_start/win_end receive intervals
+ * entries per problem; raw_offset[p] gives problem p's first value. */
+wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* win_start,
+                         int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset);
+
+/* What the last wlg_solve / wlg_solve_raw did: time by phase in
+ * milliseconds (device phases by CUDA events on the context's stream, host
+ * phases by the host clock), bytes copied host->device and device->host,
+ * and the number of engine kernels launched. */
+typedef struct {
+  double pre_ms, handoff_ms, main_ms, stitch_ms;
+  long long h2d_bytes, d2h_bytes;
+  int kernel_launches;
+} wlg_stats;
+
+wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out);
+
+/* Logical-class log-probabilities at the Nishimori temperature
+ * beta_N = ln((1-p)/p) / 2 (no counterpart in the reference): for each of
+ * n_classes normalised log g curves (energies[i], log_g[i]) with
+ * i in [offset[c], offset[c] + count[c]), log Z_c = logsumexp(log g - beta_N E)
+ * and log_probs[c] = log Z_c - logsumexp_c log Z_c. */
+wlg_status wlg_class_log_probs(const int* energies, const double* log_g, const long long* offset, const int* count,
+                               int n_classes, double prob, double* log_z, double* log_probs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -74,7 +74,7 @@ def _declare(L):
         "orc_check_finished": (None, [P, P, i32, i32]),
         "orc_replica_exchange": (None, [P] * 9 + [i32] * 6),
         "orc_prerun": (None, [i32, i32, i32, f32, C.c_char, i32, i32, i32, i32, i32, P, P, P, P, P]),
-        "orc_mainrun": (i32, [i32, i32, i32, i32, i32, i32, f32, f64, f64, i32, i32, i32, i32, i32, i64] + [P] * 6
+        "orc_mainrun": (i32, [i32, i32, i32, i32, i32, i32, f32, f64, f64, i32, i32, i32, i32, i32, i64] + [P] * 5
                         + [i32] + [P] * 8),
         "orc_stitch": (i32, [P, P, P, i32, i32, i32, i32, P, P, i32, P]),
         "orc_exact_counts": (None, [P, i32, i32, i32, P]),

@@ -242,7 +242,7 @@ MainrunOut run_mainrun(const MainrunIn& a, const uint8_t* seen, const int8_t* J,
   long long counter = 1;
   const double lim = std::exp(a.beta);
   while (max_factor - lim > 1e-10) {
-    if (o.outer >= a.max_outer) {
+    if (a.max_outer > 0 && o.outer >= a.max_outer) {
       o.status = 3;
       return o;
     }

@@ -41,8 +41,15 @@ SIGNATURES = {
     "wlg_max_int": [P, sz, P, P],
     "wlg_max_f64_nonneg": [P, sz, P, P],
     "wlg_uniforms": [u64, u64, u64, i32, P, P],
+    "wlg_context_create": [i32, sz, P],
+    "wlg_context_destroy": [P],
+    "wlg_context_last_error": [P],
+    "wlg_solve": [P, P, i32, P, P, P, i64],
+    "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
+    "wlg_last_stats": [P, P],
+    "wlg_class_log_probs": [P, P, P, P, i32, f64, P, P],
 }
-_RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p}
+_RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p}
 
 
 class WlgError(RuntimeError):
@@ -75,3 +82,129 @@ def call(name: str, *args) -> None:
 
 def version() -> str:
     return lib().wlg_version().decode()
+
+
+# ------------------------------------------------------------------ engine --
+
+WLG_OK, WLG_ERR_NEW_ENERGY, WLG_ERR_TIMEOUT, WLG_ERR_NO_LATTICE = 0, 3, 7, 5
+
+
+class Problem(C.Structure):
+    """wlg_problem: one disorder sample of one error class (see include/wlg.h)."""
+    _fields_ = [("X", i32), ("Y", i32), ("boundary", i32), ("prob", f32), ("error_class", C.c_char), ("seed", i32),
+                ("sample", i32), ("pre_walkers", i32), ("pre_intervals", i32), ("pre_iterations", i32),
+                ("intervals", i32), ("walkers_per_interval", i32), ("overlap", f32), ("alpha", f64), ("beta", f64),
+                ("iterations", i32), ("exchange_every", i32), ("exchange_mode", i32), ("global_parity", i32),
+                ("max_outer", i64)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", i32), ("new_energy", i32), ("outer_iterations", i64), ("flips", i64), ("pre_flips", i64),
+                ("n_energies", i32), ("offset", i64)]
+
+
+def problem(X, Y, *, boundary=0, prob=0.04, error_class="i", seed=12345, sample=0, pre_walkers=128,
+            pre_intervals=32, pre_iterations=1000, intervals=10, walkers_per_interval=3, overlap=0.25, alpha=0.8,
+            beta=0.001, iterations=1000, exchange_every=20, exchange_mode=1, global_parity=0, max_outer=0):
+    """A Problem with the reference's README defaults for the flags not given."""
+    return Problem(X, Y, boundary, prob, error_class.encode() if isinstance(error_class, str) else error_class, seed,
+                   sample, pre_walkers, pre_intervals, pre_iterations, intervals, walkers_per_interval, overlap,
+                   alpha, beta, iterations, exchange_every, exchange_mode, global_parity, max_outer)
+
+
+class Context:
+    """An engine context on one CUDA device (owns its stream and device buffers)."""
+
+    def __init__(self, device: int = 0, mem_budget_bytes: int = 0):
+        h = C.c_void_p()
+        call("wlg_context_create", device, mem_budget_bytes, C.byref(h))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().wlg_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, name, st):
+        if st != 0:
+            detail = lib().wlg_context_last_error(self._h).decode()
+            raise WlgError(name, st, f"{lib().wlg_status_string(st).decode()}: {detail}")
+
+    def solve(self, problems):
+        """Stitched, normalised log g per problem: list of (Result, energies, log_g) (numpy arrays)."""
+        import numpy as np
+        n = len(problems)
+        arr = (Problem * n)(*problems)
+        res = (Result * n)()
+        cap = sum(4 * p.X * p.Y + 1 for p in problems)
+        E = np.zeros(max(cap, 1), np.int32)
+        G = np.zeros(max(cap, 1), np.float64)
+        self._check("wlg_solve", lib().wlg_solve(self._h, C.cast(arr, P), n, C.cast(res, P), E.ctypes.data_as(P),
+                                                  G.ctypes.data_as(P), cap))
+        out = []
+        for r in res:
+            a, b = r.offset, r.offset + r.n_energies
+            out.append((r, E[a:b].copy(), G[a:b].copy()))
+        return out
+
+    def solve_raw(self, problems):
+        """Walker-0 log g of every window (dense, reference layout) per problem:
+        list of (Result, starts, ends, [window arrays])."""
+        import numpy as np
+        n = len(problems)
+        arr = (Problem * n)(*problems)
+        res = (Result * n)()
+        n_win = sum(p.intervals for p in problems)
+        ws = np.zeros(max(n_win, 1), np.int32)
+        we = np.zeros(max(n_win, 1), np.int32)
+        cap = sum(p.intervals * (4 * p.X * p.Y + 1) for p in problems)
+        raw = np.zeros(max(cap, 1), np.float64)
+        off = np.zeros(max(n, 1), np.int64)
+        self._check("wlg_solve_raw", lib().wlg_solve_raw(self._h, C.cast(arr, P), n, C.cast(res, P),
+                                                          ws.ctypes.data_as(P), we.ctypes.data_as(P),
+                                                          raw.ctypes.data_as(P), cap, off.ctypes.data_as(P)))
+        out, wpos = [], 0
+        for p, q in enumerate(problems):
+            s = ws[wpos:wpos + q.intervals].copy()
+            e = we[wpos:wpos + q.intervals].copy()
+            wpos += q.intervals
+            wins, pos = [], int(off[p])
+            if res[p].status in (WLG_OK, WLG_ERR_TIMEOUT):
+                for b in range(q.intervals):
+                    ln = int(e[b] - s[b] + 1)
+                    wins.append(raw[pos:pos + ln].copy())
+                    pos += ln
+            out.append((res[p], s, e, wins))
+        return out
+
+    def stats(self):
+        """What the last solve did: ms by phase, bytes copied each way, kernels launched."""
+        st = Stats()
+        call("wlg_last_stats", self._h, C.byref(st))
+        return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+
+class Stats(C.Structure):
+    _fields_ = [("pre_ms", f64), ("handoff_ms", f64), ("main_ms", f64), ("stitch_ms", f64), ("h2d_bytes", i64),
+                ("d2h_bytes", i64), ("kernel_launches", i32)]
+
+
+def class_log_probs(curves, prob):
+    """Nishimori-temperature log-probabilities of logical classes from their
+    normalised (energies, log_g) curves; returns (log_z, log_probs)."""
+    import numpy as np
+    E = np.concatenate([np.asarray(c[0], np.int32) for c in curves])
+    G = np.concatenate([np.asarray(c[1], np.float64) for c in curves])
+    cnt = np.array([len(c[0]) for c in curves], np.int32)
+    off = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int64)
+    lz = np.zeros(len(curves))
+    lp = np.zeros(len(curves))
+    call("wlg_class_log_probs", E.ctypes.data_as(P), G.ctypes.data_as(P), off.ctypes.data_as(P),
+         cnt.ctypes.data_as(P), len(curves), prob, lz.ctypes.data_as(P), lp.ctypes.data_as(P))
+    return lz, lp

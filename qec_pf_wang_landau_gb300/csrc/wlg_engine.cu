@@ -1,0 +1,634 @@
+// Batched Wang-Landau engine for sm_103a.
+//
+// k_pre_batch:  one CTA per problem runs the whole pre-run of the reference
+//               (prerun.cu:52-133) — disorder, error chain, lattice init,
+//               energy, histogram-biased walk, stored lattices — with the
+//               sample's histogram in shared memory.
+// k_main_batch: persistent kernel.  A team of threads (one per walker, a
+//               multiple of 32) takes a problem from a global work counter
+//               and runs the reference's whole main-run loop
+//               (mainrun.cu:243-383) for it without leaving the GPU: WL
+//               sweeps, flatness vote, window averaging, reset, convergence
+//               and replica exchange, then takes the next problem.
+//
+// Walker state never leaves the SM during a run:
+//   * spins bit-packed (one u64 register for N <= 64, else 32-bit words in
+//     shared memory), couplings bit-packed (registers / shared memory);
+//   * histogram (u32) and log g (f64) in shared memory, interleaved
+//     [bin][walker] so a warp's 32 walkers hit 32 distinct banks, and only
+//     over energies the lattice can reach (every 2nd or 4th value);
+//   * the current bin's log g and count cached in registers, written back
+//     only when the walker changes energy.
+// Acceptance min(1, exp(dlogg)) is decided with an FP32 exp and a guard band
+// (1e-5 relative, >6x the worst FP32 error for |dlogg| < 23); inside the
+// band, and for the site pick near a bin edge, the exact FP64 expression of
+// the reference decides, so every decision equals the reference's.
+
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "../../include/wlg.h"
+#include "wlg_engine.h"
+#include "wlg_internal.h"
+#include "wlg_lattice.cuh"
+#include "wlg_rng.cuh"
+
+namespace wlg {
+namespace {
+
+constexpr double kE = 2.718281828459045;  // std::numbers::e, mainrun.cu:56
+constexpr float kBand = 1e-5f;
+
+// ------------------------------------------------------------ pre-run -----
+
+__global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ descs, int n,
+                                                    int8_t* __restrict__ Jpool, uint8_t* __restrict__ seen_pool,
+                                                    int8_t* __restrict__ found_pool, int* __restrict__ fflag_pool)
+{
+  const int p = blockIdx.x;
+  if (p >= n) return;
+  const PreDesc d = descs[p];
+  const int N = d.N, X = d.X, Y = d.Y;
+  const int L = 4 * N + 1;
+  const int e_min = -2 * N;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned long long* hist = reinterpret_cast<unsigned long long*>(smem);
+  int* claim = reinterpret_cast<int*>(hist + L);
+  int* found = claim + d.n_int;
+  int* misc = found + d.n_int;  // [0] start energy
+  int8_t* J = reinterpret_cast<int8_t*>(misc + 4);
+  int8_t* lat = J + 2 * N;  // [walkers][N]
+
+  const int tid = threadIdx.x;
+  // disorder (wl.cu:364-386) and error chain (wl.cu:388-428, prerun.cu:56-75)
+  for (int q = tid; q < 2 * N; q += blockDim.x) {
+    Stream st;
+    st.init(key_size(d.seed, static_cast<uint64_t>(d.sample)), 0, static_cast<uint64_t>(q));
+    const double u = st.uniform();
+    J[q] = (u < d.prob) ? -1 : 1;
+  }
+  for (int q = tid; q < L; q += blockDim.x) hist[q] = 0;
+  for (int q = tid; q < d.n_int; q += blockDim.x) {
+    claim[q] = INT_MAX;
+    found[q] = 0;
+  }
+  __syncthreads();
+  if (d.error_class == 'h' || d.error_class == 'c')
+    for (int q = tid; q < Y; q += blockDim.x) J[N + q] = static_cast<int8_t>(-J[N + q]);
+  if (d.error_class == 'v' || d.error_class == 'c')
+    for (int q = tid; q < X; q += blockDim.x) J[q * Y] = static_cast<int8_t>(-J[q * Y]);
+  // lattice (wl.cu:430-457, CAS winner fixed to site 0)
+  const uint64_t key_l = key_u32(d.seed, static_cast<uint64_t>(d.sample));
+  for (int q = tid; q < N; q += blockDim.x) {
+    Stream st;
+    st.init(key_l, 1, 0);
+    const float p0 = st.uniform();
+    st.init(key_l, 1, static_cast<uint64_t>(q) + 1);
+    const double u = st.uniform();
+    lat[q] = (u < p0) ? -1 : 1;
+  }
+  __syncthreads();
+  for (int q = tid; q < 2 * N; q += blockDim.x) Jpool[d.off_J + q] = J[q];
+  const int w = tid;
+  const bool live = w < d.walkers;
+  int8_t* s = lat + static_cast<size_t>(w) * N;
+  if (live && w > 0)
+    for (int q = 0; q < N; ++q) s[q] = lat[q];
+  if (tid == 0) misc[0] = energy_i8(lat, J, X, Y, d.boundary);
+  __syncthreads();
+
+  // histogram-biased walk (wl.cu:473-560), round-synchronous
+  Stream rng;
+  int energy = misc[0];
+  if (live) rng.init(key_u32(d.seed, static_cast<uint64_t>(d.sample)), 2 + static_cast<uint64_t>(w), 0);
+  const double site_scale = (N - 1 + 0.999999);
+  bool ok = live;
+  for (int it = 0; it < d.n_iter; ++it) {
+    int hit = -1;
+    bool acc = false;
+    if (ok) {
+      const Move m = propose_i8(rng, s, J, energy, X, Y, site_scale, d.boundary);
+      const int io = energy - e_min;
+      const int in = m.new_energy - e_min;
+      const double prob = exp(static_cast<double>(hist[io]) - static_cast<double>(hist[in]));
+      const double u = rng.uniform();
+      if (u < prob) {
+        s[m.site] = static_cast<int8_t>(-s[m.site]);
+        energy = m.new_energy;
+        acc = true;
+        hit = in;
+      } else {
+        hit = io;
+      }
+    }
+    __syncthreads();
+    int bin = -1;
+    if (hit >= 0) atomicAdd(&hist[hit], 1ull);
+    if (acc) {
+      const int q = (energy - e_min) / d.len_int;
+      bin = (q < d.n_int) ? q : d.n_int - 1;
+      if (found[bin] == 0) atomicMin(&claim[bin], w);
+      else bin = -1;
+    }
+    __syncthreads();
+    if (bin >= 0 && claim[bin] == w && found[bin] == 0) {
+      found[bin] = 1;
+      int8_t* dst = found_pool + d.off_found + static_cast<long long>(bin) * N;
+      for (int q = 0; q < N; ++q) dst[q] = s[q];
+    }
+  }
+  __syncthreads();
+  for (int q = tid; q < L; q += blockDim.x) seen_pool[d.off_seen + q] = hist[q] != 0 ? 1 : 0;
+  // energies of the stored lattices (prerun.cu:123-133)
+  for (int q = tid; q < d.n_int; q += blockDim.x) {
+    fflag_pool[d.off_fflag + q] = found[q];
+    int e = 0;
+    if (found[q]) e = energy_i8(found_pool + d.off_found + static_cast<long long>(q) * N, J, X, Y, d.boundary);
+    fflag_pool[d.off_fflag + d.n_int + q] = e;
+  }
+}
+
+// ----------------------------------------------------------- main run -----
+
+struct Team {
+  int size;  // threads
+  int id;    // barrier id (1..15) or 0 for a single warp
+  __device__ __forceinline__ void sync() const
+  {
+    if (size == 32) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(size) : "memory");
+    }
+  }
+};
+
+// Site of a draw: trunc(double(u) * ((N-1) + 0.999999)) (wl.cu:63-65),
+// computed in FP32 unless the product lies within site_eps of an integer.
+__device__ __forceinline__ int pick_site(uint32_t x, const MainDesc& d)
+{
+  const float uf = unit_float(x);
+  const float pr = uf * d.site_scale_f;
+  int s = static_cast<int>(pr);
+  const float fr = pr - static_cast<float>(s);
+  if (fr < d.site_eps || fr > 1.0f - d.site_eps) s = static_cast<int>(trunc(static_cast<double>(uf) * d.site_scale));
+  return s;
+}
+
+// u < min(1, exp(delta)) with delta = logg_old - logg_new (wl.cu:1113-1116).
+__device__ __forceinline__ bool accept_move(uint32_t x, double delta)
+{
+  const float u = unit_float(x);
+  if (delta >= 0.0) return u < 1.0f;
+  const float ef = expf(static_cast<float>(delta));
+  if (u < ef * (1.0f - kBand)) return true;
+  if (u > ef * (1.0f + kBand)) return false;
+  return static_cast<double>(u) < fmin(1.0, exp(delta));
+}
+
+struct Lat {
+  uint64_t r;           // spins in a register (N <= 64)
+  uint32_t* s;          // or shared-memory words, stride P
+  int P;
+};
+
+template <bool kReg>
+__device__ __forceinline__ uint32_t spin_bit(const Lat& l, int q)
+{
+  if constexpr (kReg) {
+    return static_cast<uint32_t>(l.r >> q) & 1u;
+  } else {
+    return (l.s[(q >> 5) * l.P] >> (q & 31)) & 1u;
+  }
+}
+
+template <bool kReg>
+__device__ __forceinline__ void flip_spin(Lat& l, int q)
+{
+  if constexpr (kReg) {
+    l.r ^= 1ull << q;
+  } else {
+    l.s[(q >> 5) * l.P] ^= 1u << (q & 31);
+  }
+}
+
+template <bool kReg>
+__device__ __forceinline__ uint32_t bond_bit(uint64_t reg, const uint32_t* sm, int q)
+{
+  if constexpr (kReg) {
+    return static_cast<uint32_t>(reg >> q) & 1u;
+  } else {
+    return (sm[q >> 5] >> (q & 31)) & 1u;
+  }
+}
+
+// Energy after flipping `site` (wl.cu:52-156 on bits: a neighbour term
+// s_nb * J is -1 exactly when its spin bit and bond bit differ).
+template <bool kReg>
+__device__ __forceinline__ int energy_after_flip(const Lat& l, uint64_t JR, uint64_t JD, const uint32_t* Jr_s,
+                                                 const uint32_t* Jd_s, int site, int E, const MainDesc& d)
+{
+  const int i = static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20);
+  const int j = site - i * d.Y;
+  const int up = (i == 0 ? d.X - 1 : i - 1) * d.Y + j;
+  const int dn = (i == d.X - 1 ? 0 : i + 1) * d.Y + j;
+  const int lf = i * d.Y + (j == 0 ? d.Y - 1 : j - 1);
+  const int rt = i * d.Y + (j == d.Y - 1 ? 0 : j + 1);
+  const int t_up = static_cast<int>(spin_bit<kReg>(l, up) ^ bond_bit<kReg>(JD, Jd_s, up));
+  const int t_lf = static_cast<int>(spin_bit<kReg>(l, lf) ^ bond_bit<kReg>(JR, Jr_s, lf));
+  const int t_dn = static_cast<int>(spin_bit<kReg>(l, dn) ^ bond_bit<kReg>(JD, Jd_s, site));
+  const int t_rt = static_cast<int>(spin_bit<kReg>(l, rt) ^ bond_bit<kReg>(JR, Jr_s, site));
+  int sigma;
+  if (d.boundary == 0) {
+    sigma = 4 - 2 * (t_up + t_lf + t_dn + t_rt);
+  } else {
+    sigma = (i > 0 ? 1 - 2 * t_up : 0) + (j > 0 ? 1 - 2 * t_lf : 0) + (i < d.X - 1 ? 1 - 2 * t_dn : 0) +
+            (j < d.Y - 1 ? 1 - 2 * t_rt : 0);
+  }
+  const int s = 1 - 2 * static_cast<int>(spin_bit<kReg>(l, site));
+  return E + 2 * s * sigma;
+}
+
+__device__ __forceinline__ bool mask_has(const uint32_t* mask, int c) { return (mask[c >> 5] >> (c & 31)) & 1u; }
+
+template <bool kReg>
+__device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base,
+                            const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
+                            const int* __restrict__ winpool, const uint32_t* __restrict__ maskpool,
+                            double* __restrict__ outpool, MainResult* __restrict__ results,
+                            uint32_t* __restrict__ dumppool)
+{
+  const int P = team.size;
+  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg);
+  double* G = reinterpret_cast<double*>(base + lay.off_G);
+  uint32_t* H = reinterpret_cast<uint32_t*>(base + lay.off_H);
+  uint32_t* lat_s = reinterpret_cast<uint32_t*>(base + lay.off_lat);
+  int* E_s = reinterpret_cast<int*>(base + lay.off_E);
+  int* perm = reinterpret_cast<int*>(base + lay.off_perm);
+  uint32_t* mask = reinterpret_cast<uint32_t*>(base + lay.off_mask);
+  uint32_t* Js = reinterpret_cast<uint32_t*>(base + lay.off_J);
+  double* fwin = reinterpret_cast<double*>(base + lay.off_f);
+  int* cond = reinterpret_cast<int*>(base + lay.off_cond);
+  int* flat = reinterpret_cast<int*>(base + lay.off_flat);
+  int* win = reinterpret_cast<int*>(base + lay.off_win);  // start, end, base, Lb, E0
+  int* misc = reinterpret_cast<int*>(base + lay.off_misc);
+  const int I = d.I, W = d.W;
+  int* w_start = win;
+  int* w_end = win + I;
+  int* w_base = win + 2 * I;
+  int* w_len = win + 3 * I;
+
+  // ---- load the problem
+  for (int q = t; q < d.nwM; q += P) mask[q] = maskpool[d.off_mask + q];
+  for (int q = t; q < 2 * d.nwL; q += P) Js[q] = Jpool[d.off_J + q];
+  for (int q = t; q < 5 * I; q += P) win[q] = winpool[d.off_win + q];
+  for (int q = t; q < I; q += P) {
+    fwin[q] = kE;
+    cond[q] = 0;
+    flat[q] = 0;
+  }
+  for (int c = 0; c < d.L; ++c) {
+    G[c * P + t] = 0.0;
+    H[c * P + t] = 0u;
+  }
+  if (t < 8) misc[t] = 0;
+  const bool live = t < d.nwalk;
+  const int b = live ? t / W : 0;
+  const int w = t - b * W;
+  perm[t] = w;
+  team.sync();
+
+  uint64_t JR = 0, JD = 0;
+  if constexpr (kReg) {
+    JR = Js[0] | (d.nwL > 1 ? static_cast<uint64_t>(Js[1]) << 32 : 0ull);
+    JD = Js[d.nwL] | (d.nwL > 1 ? static_cast<uint64_t>(Js[d.nwL + 1]) << 32 : 0ull);
+  }
+  const uint32_t* Jr_s = Js;
+  const uint32_t* Jd_s = Js + d.nwL;
+  Lat lt;
+  lt.P = P;
+  lt.s = lat_s + t;
+  lt.r = 0;
+  if (live) {
+    const uint32_t* src = latpool + d.off_lat + static_cast<long long>(b) * d.nwL;
+    if constexpr (kReg) {
+      lt.r = src[0] | (d.nwL > 1 ? static_cast<uint64_t>(src[1]) << 32 : 0ull);
+    } else {
+      for (int q = 0; q < d.nwL; ++q) lat_s[q * P + t] = src[q];
+    }
+  }
+  int E = live ? win[4 * I + b] : 0;
+  Stream rng;
+  rng.init(d.key_wl, static_cast<uint64_t>(t), 0);
+  const bool keys_differ = d.key_ex != static_cast<uint64_t>(d.key_wl);
+  const double reset_lim = exp(d.beta);  // wl.cu:609
+  const int lo = live ? w_start[b] : 0, hi = live ? w_end[b] : 0, bb = live ? w_base[b] : 0;
+  const int step_mask = (1 << d.lg) - 1;
+
+  long long outer = 0;
+  long long counter = 1;
+  int status = WLG_OK;
+  team.sync();
+
+  for (;;) {
+    if (d.max_outer > 0 && outer >= d.max_outer) {
+      status = WLG_ERR_TIMEOUT;
+      break;
+    }
+    // ---- WL sweep (wl.cu:1077-1175)
+    if (live) {
+      const bool frozen = cond[b] != 0;
+      const double lnf = log(fwin[b]);
+      int c_cur = (E - bb) >> d.lg;
+      double g_cur = G[c_cur * P + t];
+      uint32_t h_cur = H[c_cur * P + t];
+      for (int it = 0; it < d.n_iter; ++it) {
+        const int site = pick_site(rng.raw(), d);
+        const int En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
+        const int rel = En - d.e_min;
+        if (rel < 0 || En > d.e_max || (rel & step_mask) != 0 || !mask_has(mask, rel >> d.lg)) {
+          misc[1] = 1;  // found a new energy (wl.cu:1091-1104): the problem stops
+          misc[2] = En;
+          break;
+        }
+        if (En < lo || En > hi) {
+          if (!frozen) {
+            g_cur += lnf;
+            h_cur += 1u;
+          }
+          continue;
+        }
+        const int c_new = (En - bb) >> d.lg;
+        const double g_new = (c_new == c_cur) ? g_cur : G[c_new * P + t];
+        const bool acc = accept_move(rng.raw(), g_cur - g_new);
+        if (frozen) {
+          if (acc) {
+            flip_spin<kReg>(lt, site);
+            E = En;
+            c_cur = c_new;
+            g_cur = g_new;
+          }
+          continue;
+        }
+        if (acc) {
+          flip_spin<kReg>(lt, site);
+          if (c_new != c_cur) {
+            G[c_cur * P + t] = g_cur;
+            H[c_cur * P + t] = h_cur;
+            g_cur = g_new;
+            h_cur = H[c_new * P + t];
+            c_cur = c_new;
+          }
+          E = En;
+        }
+        g_cur += lnf;
+        h_cur += 1u;
+      }
+      if (!frozen) {
+        G[c_cur * P + t] = g_cur;
+        H[c_cur * P + t] = h_cur;
+      }
+    }
+    team.sync();
+    ++outer;
+    if (misc[1] != 0) {
+      status = WLG_ERR_NEW_ENERGY;
+      break;
+    }
+    // ---- flatness (wl.cu:892-967)
+    if (live && cond[b] == 0) {
+      const int cb = (bb - d.e_min) >> d.lg;
+      uint32_t mn = 2147483647u;
+      unsigned long long sum = 0;
+      int cnt = 0;
+      for (int c = 0; c < w_len[b]; ++c) {
+        if (!mask_has(mask, cb + c)) continue;
+        const uint32_t v = H[c * P + t];
+        mn = v < mn ? v : mn;
+        sum += v;
+        ++cnt;
+      }
+      if (cnt > 0 && static_cast<double>(mn) >= d.alpha * (static_cast<double>(sum) / cnt)) atomicAdd(&flat[b], 1);
+    }
+    team.sync();
+    if (live && cond[b] == 0 && flat[b] == W) {
+      for (int c = 0; c < d.L; ++c) H[c * P + t] = 0u;
+    }
+    team.sync();
+    if (t < I && cond[t] == 0 && flat[t] == W) {
+      fwin[t] = sqrt(fwin[t]);
+      cond[t] = 1;
+    }
+    team.sync();
+    // ---- window averages (wl.cu:710-783 + :969-1031)
+    for (int q = t; q < I * d.L; q += P) {
+      const int wb = q / d.L;
+      const int c = q - wb * d.L;
+      if (cond[wb] != 1 || c >= w_len[wb]) continue;
+      double avg = 0.0;
+      if (mask_has(mask, ((w_base[wb] - d.e_min) >> d.lg) + c)) {
+        for (int v = 0; v < W; ++v) avg += G[c * P + wb * W + v] / W;
+      }
+      for (int v = 0; v < W; ++v) G[c * P + wb * W + v] = avg;
+    }
+    team.sync();
+    // ---- reset and convergence (wl.cu:596-613, :662-708, mainrun.cu:243, :342-344)
+    if (t < I) {
+      if (cond[t] == 1 && fwin[t] > reset_lim) cond[t] = 0;
+      flat[t] = 0;
+    }
+    team.sync();
+    bool done = true;
+    double fmax = 0.0;
+    for (int q = 0; q < I; ++q) {
+      done = done && cond[q] == 1;
+      fmax = fmax > fwin[q] ? fmax : fwin[q];
+    }
+    const bool stop = !(fmax - d.loop_lim > 1e-10);
+    // ---- replica exchange (wl.cu:785-890)
+    if (!done && counter % d.exch_every == 0) {
+      if (live) {
+        E_s[t] = E;
+        if constexpr (kReg) {
+          lat_s[t] = static_cast<uint32_t>(lt.r);
+          lat_s[P + t] = static_cast<uint32_t>(lt.r >> 32);
+        }
+        if (keys_differ) rng.init(d.key_ex, static_cast<uint64_t>(t), rng.pos);
+      }
+      const int nw = kReg ? 2 : d.nwL;
+      for (int pass = 0; pass < 2; ++pass) {
+        const int even = pass == 0;
+        team.sync();
+        const int par = (b + d.parity_base) & 1;
+        const bool active = live && b < I - 1 && ((even && par == 0) || (!even && par == 1));
+        if (active && w == 0) {  // Fisher-Yates by the window's first walker
+          for (int i = W - 1; i > 0; --i) {
+            double u = rng.uniform();
+            u *= (i + 0.999999);
+            const int r = static_cast<int>(trunc(u));
+            const int tmp = perm[t + i];
+            perm[t + i] = perm[t + r];
+            perm[t + r] = tmp;
+          }
+        }
+        team.sync();
+        if (active) {
+          const int o = (b + 1) * W + perm[t];
+          const int et = E_s[t], eo = E_s[o];
+          if (et >= w_start[b + 1] && et <= w_end[b + 1] && eo >= w_start[b] && eo <= w_end[b]) {
+            const int nb = w_base[b + 1];
+            const double gi_x = G[((et - bb) >> d.lg) * P + t];
+            const double gi_y = G[((eo - bb) >> d.lg) * P + t];
+            const double gj_y = G[((eo - nb) >> d.lg) * P + o];
+            const double gj_x = G[((et - nb) >> d.lg) * P + o];
+            const double prob = fmin(1.0, exp(gi_x - gi_y) * exp(gj_y - gj_x));
+            if (rng.uniform() < prob) {
+              E_s[t] = eo;
+              E_s[o] = et;
+              for (int q = 0; q < nw; ++q) {
+                const uint32_t a = lat_s[q * P + t];
+                lat_s[q * P + t] = lat_s[q * P + o];
+                lat_s[q * P + o] = a;
+              }
+            }
+          }
+        }
+      }
+      team.sync();
+      if (live) {
+        E = E_s[t];
+        if constexpr (kReg) lt.r = lat_s[t] | static_cast<uint64_t>(lat_s[P + t]) << 32;
+        if (keys_differ) rng.init(d.key_wl, static_cast<uint64_t>(t), rng.pos);
+      }
+    }
+    if (d.exch_mode == 1) ++counter;
+    team.sync();
+    if (stop) break;
+  }
+
+  // ---- results
+  if (live && w == 0) {
+    for (int c = 0; c < d.L; ++c) outpool[d.off_out + static_cast<long long>(b) * d.L + c] = G[c * P + t];
+  }
+  if (d.off_dump >= 0 && live) {
+    const long long per = dump_words_per_walker(d.nwL, d.L);
+    uint32_t* o = dumppool + d.off_dump + per * t;
+    o[0] = static_cast<uint32_t>(E);
+    o[1] = static_cast<uint32_t>(rng.pos);
+    o[2] = static_cast<uint32_t>(rng.pos >> 32);
+    for (int q = 0; q < d.nwL; ++q) {
+      if constexpr (kReg) {
+        o[3 + q] = static_cast<uint32_t>(lt.r >> (32 * q));
+      } else {
+        o[3 + q] = lat_s[q * P + t];
+      }
+    }
+    for (int c = 0; c < d.L; ++c) {
+      const double g = G[c * P + t];
+      const unsigned long long gb = static_cast<unsigned long long>(__double_as_longlong(g));
+      o[3 + d.nwL + 2 * c] = static_cast<uint32_t>(gb);
+      o[3 + d.nwL + 2 * c + 1] = static_cast<uint32_t>(gb >> 32);
+      o[3 + d.nwL + 2 * d.L + c] = H[c * P + t];
+    }
+  }
+  if (t == 0) {
+    MainResult r;
+    r.status = status;
+    r.new_energy = misc[2];
+    r.outer = outer;
+    r.flips = outer * static_cast<long long>(d.nwalk) * d.n_iter;
+    results[p] = r;
+  }
+  team.sync();
+}
+
+template <bool kReg, int kMaxThreads>
+__global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __restrict__ descs, const int* __restrict__ order,
+                                                     int n, int team_size, int team_bytes, int* __restrict__ next,
+                                                     const uint32_t* __restrict__ Jpool,
+                                                     const uint32_t* __restrict__ latpool,
+                                                     const int* __restrict__ winpool,
+                                                     const uint32_t* __restrict__ maskpool,
+                                                     double* __restrict__ outpool, MainResult* __restrict__ results,
+                                                     uint32_t* __restrict__ dumppool)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tix = threadIdx.x / team_size;
+  Team team{team_size, team_size == 32 ? 0 : 1 + tix};
+  const int t = threadIdx.x - tix * team_size;
+  unsigned char* base = smem + static_cast<size_t>(tix) * team_bytes;
+  int* slot = reinterpret_cast<int*>(base + team_bytes - 16);
+  for (;;) {
+    if (t == 0) *slot = atomicAdd(next, 1);
+    team.sync();
+    const int q = *slot;
+    team.sync();
+    if (q >= n) return;
+    const int p = order[q];
+    const MainDesc d = descs[p];
+    run_problem<kReg>(d, p, team, t, base, Jpool, latpool, winpool, maskpool, outpool, results, dumppool);
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ launchers ----
+
+wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem, int8_t* Jpool, uint8_t* seen_pool,
+                            int8_t* found_pool, int* fflag_pool, cudaStream_t s)
+{
+  if (n == 0) return WLG_OK;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_pre_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return WLG_ERR_CUDA;
+  }
+  k_pre_batch<<<n, threads, smem, s>>>(d_descs, n, Jpool, seen_pool, found_pool, fflag_pool);
+  return launch_status();
+}
+
+template <bool kReg, int kMaxThreads>
+struct MainKernel {
+  static decltype(&k_main_batch<kReg, kMaxThreads>) fn() { return &k_main_batch<kReg, kMaxThreads>; }
+};
+
+using MainFn = void (*)(const MainDesc*, const int*, int, int, int, int*, const uint32_t*, const uint32_t*, const int*,
+                        const uint32_t*, double*, MainResult*, uint32_t*);
+
+MainFn main_fn(bool reg, int cta_threads)
+{
+  if (cta_threads <= 256) return reg ? MainKernel<true, 256>::fn() : MainKernel<false, 256>::fn();
+  return reg ? MainKernel<true, 1024>::fn() : MainKernel<false, 1024>::fn();
+}
+
+// Returns the number of resident CTAs the launch may use (0 if the
+// configuration does not fit).
+int main_batch_capacity(bool reg, int cta_threads, int smem)
+{
+  MainFn fn = main_fn(reg, cta_threads);
+  int per_sm = 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, cta_threads, smem) != cudaSuccess) return 0;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return per_sm * sms;
+}
+
+wlg_status launch_main_batch(bool reg, const MainDesc* d_descs, const int* d_order, int n, int team_size,
+                             int team_bytes, int teams_per_cta, int grid, int* d_next, const uint32_t* Jpool,
+                             const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
+                             MainResult* results, uint32_t* dumppool, cudaStream_t s)
+{
+  if (n == 0) return WLG_OK;
+  const int threads = team_size * teams_per_cta;
+  const int smem = team_bytes * teams_per_cta;
+  MainFn fn = main_fn(reg, threads);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return WLG_ERR_CUDA;
+  fn<<<grid, threads, smem, s>>>(d_descs, d_order, n, team_size, team_bytes, d_next, Jpool, latpool, winpool,
+                                 maskpool, outpool, results, dumppool);
+  return launch_status();
+}
+
+}  // namespace wlg

@@ -1,0 +1,117 @@
+// Batched engine: descriptors shared by the device kernels (wlg_engine.cu)
+// and the host pipeline (wlg_engine_host.cpp).  Not part of the C ABI.
+//
+// A "problem" is one disorder sample of one error class: the reference runs
+// R of them per invocation of prerun/mainrun, keyed by `seed + sample`.  The
+// engine runs thousands of heterogeneous problems per launch.
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define WLG_HD __host__ __device__
+#else
+#define WLG_HD
+#endif
+
+namespace wlg {
+
+// ------------------------------------------------------------ pre-run -----
+// One CTA per problem: disorder, error chain, lattice init, energy,
+// histogram-biased walk, stored lattices and their energies, fused.
+struct PreDesc {
+  int X, Y, N, boundary;
+  float prob;
+  int error_class;  // 'i', 'h', 'v', 'c'
+  int seed, sample;
+  int walkers;      // <= 1024
+  int n_int;        // coarse bins for stored lattices
+  int len_int;      // coarse bin width (interval.cpp with overlap 1)
+  int n_iter;
+  long long off_J;      // int8 [2N]
+  long long off_seen;   // uint8 [4N+1]
+  long long off_found;  // int8 [n_int][N]
+  long long off_fflag;  // int [n_int] flags, then int [n_int] energies
+  int smem;             // dynamic shared memory of the CTA
+};
+
+// ----------------------------------------------------------- main run -----
+// One team of threads per problem (one thread per walker, team size a
+// multiple of 32).  Walker state lives in registers and the team's shared
+// memory for the whole run.
+struct MainDesc {
+  int X, Y, N, boundary;
+  int I, W, nwalk, team;
+  int e_min, e_max, lg;   // spectrum range and log2 of the energy step
+  int L;                  // compact bins per walker (max over windows)
+  int n_iter, exch_every, exch_mode, parity_base;
+  double alpha, beta, loop_lim;  // loop_lim: exp(beta) as the host computes it
+  uint32_t key_wl;               // Philox key of the WL sweeps (wl.cu:1074)
+  uint64_t key_ex;               // Philox key of the exchange (wl.cu:796, :875)
+  uint32_t site_magic;           // ceil(2^20 / Y): site / Y = site * magic >> 20
+  float site_scale_f, site_eps;
+  double site_scale;             // (N - 1) + 0.999999, wl.cu:64
+  long long max_outer;           // 0 = no cap
+  int nwL;                       // 32-bit words per lattice
+  int nwM;                       // 32-bit words of the compact spectrum mask
+  long long off_J;               // words: right bonds [nwL], down bonds [nwL]
+  long long off_lat;             // words: start lattice of each window [I][nwL]
+  long long off_win;             // ints: start[I], end[I], base[I], Lb[I], E0[I]
+  long long off_mask;            // words [nwM]
+  long long off_out;             // doubles: [I][L] walker-0 log g (compact)
+  long long off_dump;            // per-walker dump slot (tests), -1 = none
+};
+
+// Per-problem result of the main run.
+struct MainResult {
+  int status;  // WLG_OK, WLG_ERR_NEW_ENERGY, WLG_ERR_TIMEOUT
+  int new_energy;
+  long long outer;
+  long long flips;
+};
+
+// Team shared-memory layout of a problem (bytes, 16-byte aligned pieces).
+struct TeamLayout {
+  int off_G, off_H, off_lat, off_E, off_perm, off_mask, off_J, off_f, off_cond, off_flat, off_win, off_misc;
+  int bytes;
+};
+
+WLG_HD inline int align16(int x) { return (x + 15) & ~15; }
+
+WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, bool reg_lattice)
+{
+  TeamLayout t{};
+  int o = 0;
+  t.off_G = o;
+  o = align16(o + 8 * L * team);
+  t.off_H = o;
+  o = align16(o + 4 * L * team);
+  t.off_lat = o;
+  o = align16(o + 4 * (reg_lattice ? 2 : nwL) * team);
+  t.off_E = o;
+  o = align16(o + 4 * team);
+  t.off_perm = o;
+  o = align16(o + 4 * team);
+  t.off_mask = o;
+  o = align16(o + 4 * nwM);
+  t.off_J = o;
+  o = align16(o + 4 * 2 * nwL);
+  t.off_f = o;
+  o = align16(o + 8 * I);
+  t.off_cond = o;
+  o = align16(o + 4 * I);
+  t.off_flat = o;
+  o = align16(o + 4 * I);
+  t.off_win = o;
+  o = align16(o + 4 * 5 * I);
+  t.off_misc = o;
+  o = align16(o + 4 * 8);
+  t.bytes = o;
+  return t;
+}
+
+// Dump of one problem's final walker state (parity tests), per walker:
+// E, RNG position, lattice words, then the compact log g [L] and H [L].
+WLG_HD inline long long dump_words_per_walker(int nwL, int L) { return 1 + 2 + nwL + 2 * L + L; }
+
+}  // namespace wlg

@@ -1,0 +1,768 @@
+// Host side of the batched engine (C++20): the pre-run -> main-run hand-off
+// of the reference (file_io.cpp:558-659, mainrun.cu:79-113) for many
+// heterogeneous problems, grouping into persistent launches, result
+// stitching (result_handling.cpp:26-431) and the C ABI of wlg.h, part 2.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <numbers>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/wlg.h"
+#include "wlg_engine.h"
+#include "wlg_internal.h"
+#include "wlg_rng.cuh"
+
+namespace wlg {
+
+wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem, int8_t* Jpool, uint8_t* seen_pool,
+                            int8_t* found_pool, int* fflag_pool, cudaStream_t s);
+int main_batch_capacity(bool reg, int cta_threads, int smem);
+wlg_status launch_main_batch(bool reg, const MainDesc* d_descs, const int* d_order, int n, int team_size,
+                             int team_bytes, int teams_per_cta, int grid, int* d_next, const uint32_t* Jpool,
+                             const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
+                             MainResult* results, uint32_t* dumppool, cudaStream_t s);
+
+// ---------------------------------------------------------- energy windows --
+// interval.cpp:5-41: window length from a float division truncated toward
+// zero, step = trunc(overlap * length), the last window ends at e_max.
+wlg_status make_windows(int e_min, int e_max, int n, float overlap, std::vector<int>& start, std::vector<int>& end)
+{
+  if (n <= 0) return WLG_ERR_INVALID;
+  if (overlap > 1 || overlap < 0) return WLG_ERR_INVALID;
+  const int range = e_max - e_min + 1;
+  const int len =
+    static_cast<int>(static_cast<float>(range) / (1.0F + overlap * static_cast<float>(static_cast<unsigned>(n) - 1)));
+  const int step = static_cast<int>(overlap * static_cast<float>(len));
+  start.assign(static_cast<size_t>(n), 0);
+  end.assign(static_cast<size_t>(n), 0);
+  int s = e_min;
+  for (int b = 0; b < n; ++b) {
+    start[b] = s;
+    end[b] = (b + 1 < n) ? s + len - 1 : e_max;
+    if (start[b] >= end[b]) return WLG_ERR_EMPTY_WINDOW;
+    s += step;
+  }
+  return WLG_OK;
+}
+
+namespace {
+
+int energy_host(const int8_t* s, const int8_t* J, int X, int Y, int boundary)
+{
+  const int N = X * Y;
+  int acc = 0;
+  for (int i = 0; i < X; ++i)
+    for (int j = 0; j < Y; ++j) {
+      const int im = (i - 1 >= 0) ? i - 1 : X - 1;
+      const int jm = (j - 1 >= 0) ? j - 1 : Y - 1;
+      int up = s[im * Y + j] * J[N + im * Y + j];
+      int left = s[i * Y + jm] * J[i * Y + jm];
+      if (boundary == 1) {
+        if (i == 0) up = 0;
+        if (j == 0) left = 0;
+      }
+      acc += s[i * Y + j] * (up + left);
+    }
+  return -acc;
+}
+
+// ----------------------------------------------------------------- stitching --
+
+using Curve = std::map<int, double>;
+
+std::tuple<int, double> best_shared_key(const Curve& a, const Curve& b)
+{
+  int key = std::numeric_limits<int>::max();
+  double best = std::numeric_limits<double>::max();
+  auto x = a.begin();
+  auto y = b.begin();
+  while (x != a.end() && y != b.end()) {
+    if (x->first == y->first) {
+      const auto xn = std::next(x), yn = std::next(y);
+      if (xn != a.end() && yn != b.end()) {  // keys without a successor have no slope
+        const double dx = (xn->second - x->second) / (xn->first - x->first);
+        const double dy = (yn->second - y->second) / (yn->first - y->first);
+        const double d = std::abs(dx - dy);
+        if (d < best) {
+          best = d;
+          key = x->first;
+        }
+      }
+      ++x;
+      ++y;
+    } else if (x->first < y->first) {
+      ++x;
+    } else {
+      ++y;
+    }
+  }
+  return {key, best};
+}
+
+Curve cut(const Curve& c, int e, bool below)
+{
+  Curve o;
+  for (const auto& [k, v] : c)
+    if ((below && k < e) || (!below && k >= e)) o.emplace(k, v);
+  return o;
+}
+
+}  // namespace
+
+// result_handling.cpp:368-431.  `windows[b]` holds walker 0's nonzero log g
+// of window b.  Output: normalised (E, log g) pairs, logsumexp = X*Y*ln 2.
+wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<std::pair<int, double>>& out)
+{
+  const size_t I = windows.size();
+  for (auto& c : windows) {
+    double mn = std::numeric_limits<double>::max();
+    for (const auto& kv : c) mn = std::min(mn, kv.second);
+    if (mn == std::numeric_limits<double>::max()) mn = 0;
+    for (auto& kv : c) kv.second -= mn;
+  }
+  std::vector<std::pair<int, int>> keys;  // (next window, stitch energy)
+  for (size_t i = 0; i + 1 < I; ++i) {
+    int best_key = std::numeric_limits<int>::max();
+    double best = std::numeric_limits<double>::max();
+    int best_win = -1;
+    for (size_t j = i + 1; j < I; ++j) {
+      const auto [key, d] = best_shared_key(windows[i], windows[j]);
+      if (key == std::numeric_limits<int>::max()) break;
+      if (d < best) {
+        best = d;
+        best_key = key;
+        best_win = static_cast<int>(j);
+      }
+    }
+    if (best_win >= 0) keys.emplace_back(best_win, best_key);
+  }
+  std::vector<std::pair<int, int>> kept;  // drop keys that a later key undercuts
+  for (size_t i = 0; i < keys.size(); ++i) {
+    bool keep = true;
+    for (size_t j = i + 1; j < keys.size(); ++j)
+      if (keys[j].second <= keys[i].second) keep = false;
+    if (keep) kept.push_back(keys[i]);
+  }
+  if (kept.empty() && I > 1) return WLG_ERR_STITCH;
+  std::vector<std::pair<int, int>> chain;  // smallest energy per next window
+  for (const auto& kv : kept) {
+    if (!chain.empty() && chain.back().first == kv.first) {
+      chain.back().second = std::min(chain.back().second, kv.second);
+    } else {
+      chain.push_back(kv);
+    }
+  }
+  for (size_t i = 0; i < chain.size(); ++i) {
+    const int e = chain[i].second;
+    const size_t nxt = static_cast<size_t>(chain[i].first);
+    const size_t prev = (i == 0) ? 0 : static_cast<size_t>(chain[i - 1].first);
+    const auto a = windows[prev].find(e);
+    const auto b = windows[nxt].find(e);
+    if (a == windows[prev].end() || b == windows[nxt].end()) return WLG_ERR_STITCH;
+    const double shift = a->second - b->second;
+    for (auto& kv : windows[nxt]) kv.second += shift;
+  }
+  std::vector<Curve> parts;
+  if (chain.empty()) {
+    parts.push_back(windows[0]);
+  } else {
+    auto first = cut(windows[0], chain[0].second, true);
+    if (!first.empty()) parts.push_back(std::move(first));
+    for (size_t i = 1; i < chain.size(); ++i) {
+      auto m = cut(cut(windows[static_cast<size_t>(chain[i - 1].first)], chain[i].second, true),
+                   chain[i - 1].second, false);
+      if (!m.empty()) parts.push_back(std::move(m));
+    }
+    auto last = cut(windows[static_cast<size_t>(chain.back().first)], chain.back().second, false);
+    if (!last.empty()) parts.push_back(std::move(last));
+  }
+  double mx = -std::numeric_limits<double>::infinity();
+  for (const auto& c : parts)
+    for (const auto& kv : c) mx = std::max(mx, kv.second);
+  double se = 0.0;
+  for (const auto& c : parts)
+    for (const auto& kv : c) se += std::exp(kv.second - mx);
+  const double shift = mx + std::log(se);
+  const double l2 = std::log(2) * static_cast<double>(X) * static_cast<double>(Y);
+  out.clear();
+  for (const auto& c : parts)
+    for (const auto& kv : c) out.emplace_back(kv.first, kv.second + l2 - shift);
+  return WLG_OK;
+}
+
+}  // namespace wlg
+
+// ------------------------------------------------------------------ context --
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+struct wlg_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  size_t used = 0;
+  DevBuf pre_desc, J8, seen, found, fflag, main_desc, order, next, Jw, latw, win, mask, out, res, dump;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float t_pre = 0, t_main = 0;
+  double t_handoff = 0, t_stitch = 0;
+  long long h2d = 0, d2h = 0;
+  int launches = 0;
+  std::string err;
+};
+
+namespace {
+
+using wlg::MainDesc;
+using wlg::MainResult;
+using wlg::PreDesc;
+
+wlg_status fail(wlg_context* ctx, wlg_status st, const std::string& msg)
+{
+  ctx->err = msg;
+  return st;
+}
+
+wlg_status grow(wlg_context* ctx, DevBuf& b, size_t bytes)
+{
+  if (bytes <= b.cap) return WLG_OK;
+  bytes = std::max<size_t>(bytes, 256);
+  if (b.p != nullptr) {
+    cudaFree(b.p);
+    ctx->used -= b.cap;
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  if (ctx->budget != 0 && ctx->used + bytes > ctx->budget) return fail(ctx, WLG_ERR_OOM, "device memory budget");
+  const cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) return fail(ctx, wlg::cuda_status(e), cudaGetErrorString(e));
+  b.cap = bytes;
+  ctx->used += bytes;
+  return WLG_OK;
+}
+
+template <typename T>
+wlg_status upload(wlg_context* ctx, DevBuf& b, const std::vector<T>& h)
+{
+  const size_t bytes = h.size() * sizeof(T);
+  wlg_status st = grow(ctx, b, bytes);
+  if (st != WLG_OK || bytes == 0) return st;
+  const cudaError_t e = cudaMemcpyAsync(b.p, h.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
+  ctx->h2d += static_cast<long long>(bytes);
+  return e == cudaSuccess ? WLG_OK : fail(ctx, WLG_ERR_CUDA, cudaGetErrorString(e));
+}
+
+template <typename T>
+wlg_status download(wlg_context* ctx, const DevBuf& b, std::vector<T>& h)
+{
+  if (h.empty()) return WLG_OK;
+  const cudaError_t e = cudaMemcpyAsync(h.data(), b.p, h.size() * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream);
+  ctx->d2h += static_cast<long long>(h.size() * sizeof(T));
+  return e == cudaSuccess ? WLG_OK : fail(ctx, WLG_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int round32(int x) { return (x + 31) / 32 * 32; }
+
+wlg_status check_problem(const wlg_problem& q)
+{
+  if (q.X < 2 || q.Y < 2 || q.X * q.Y > 4096 || (q.boundary != 0 && q.boundary != 1)) return WLG_ERR_INVALID;
+  if (q.pre_walkers <= 0 || q.pre_walkers > 1024 || q.pre_intervals <= 0 || q.pre_iterations < 0)
+    return WLG_ERR_INVALID;
+  if (q.intervals <= 0 || q.walkers_per_interval <= 0 || q.intervals * q.walkers_per_interval > 1024)
+    return WLG_ERR_INVALID;
+  if (q.overlap < 0 || q.overlap > 1 || q.iterations <= 0 || q.exchange_every <= 0 || q.max_outer < 0)
+    return WLG_ERR_INVALID;
+  if (q.exchange_mode != 0 && q.exchange_mode != 1) return WLG_ERR_INVALID;
+  if (q.Y > 1024) return WLG_ERR_INVALID;
+  return WLG_OK;
+}
+
+struct Prepared {
+  std::vector<MainDesc> main;          // problems that reach the main run
+  std::vector<int> main_problem;       // index into the batch
+  std::vector<std::vector<int>> starts, ends;  // per batch problem
+  std::vector<int> lg, base_off;       // per main entry: log2 step, offset of w_base in win pool
+};
+
+// The whole batch up to the main-run results.
+wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_result* results,
+                     std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
+                     std::vector<int>& win_host)
+{
+  using clock = std::chrono::steady_clock;
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  ctx->t_pre = ctx->t_main = 0;
+  ctx->t_handoff = ctx->t_stitch = 0;
+  for (int p = 0; p < n; ++p) {
+    if (check_problem(probs[p]) != WLG_OK) return fail(ctx, WLG_ERR_INVALID, "invalid problem " + std::to_string(p));
+    std::memset(&results[p], 0, sizeof(wlg_result));
+  }
+  // ---------------- pre-run
+  std::vector<PreDesc> pd(static_cast<size_t>(n));
+  long long oJ = 0, oS = 0, oF = 0, oG = 0;
+  int threads = 32, smem = 0;
+  for (int p = 0; p < n; ++p) {
+    const wlg_problem& q = probs[p];
+    PreDesc& d = pd[p];
+    d.X = q.X;
+    d.Y = q.Y;
+    d.N = q.X * q.Y;
+    d.boundary = q.boundary;
+    d.prob = q.prob;
+    d.error_class = q.error_class == 'I' ? 'i' : q.error_class;
+    d.seed = q.seed;
+    d.sample = q.sample;
+    d.walkers = q.pre_walkers;
+    d.n_int = q.pre_intervals;
+    std::vector<int> s, e;
+    // prerun.cu:23-25: coarse bins of [-2N, 2N] with overlap 1
+    if (wlg::make_windows(-2 * d.N, 2 * d.N, q.pre_intervals, 1.0F, s, e) != WLG_OK)
+      return fail(ctx, WLG_ERR_INVALID, "pre-run intervals produce empty bins");
+    d.len_int = e[0] - s[0] + 1;
+    d.n_iter = q.pre_iterations;
+    d.off_J = oJ;
+    d.off_seen = oS;
+    d.off_found = oF;
+    d.off_fflag = oG;
+    oJ += 2 * d.N;
+    oS += 4 * d.N + 1;
+    oF += static_cast<long long>(d.n_int) * d.N;
+    oG += 2 * d.n_int;
+    d.smem = wlg::align16(8 * (4 * d.N + 1) + 8 * d.n_int + 16 + 2 * d.N + d.walkers * d.N);
+    smem = std::max(smem, d.smem);
+    threads = std::max(threads, round32(d.walkers));
+    results[p].pre_flips = static_cast<long long>(q.pre_walkers) * q.pre_iterations;
+  }
+  if (smem > 227 * 1024) return fail(ctx, WLG_ERR_INVALID, "pre-run walkers x lattice too large for shared memory");
+  wlg_status st;
+  if ((st = upload(ctx, ctx->pre_desc, pd)) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->J8, static_cast<size_t>(oJ))) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->seen, static_cast<size_t>(oS))) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->found, static_cast<size_t>(oF))) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->fflag, static_cast<size_t>(oG) * sizeof(int))) != WLG_OK) return st;
+  cudaMemsetAsync(ctx->found.p, 0, static_cast<size_t>(oF), ctx->stream);
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  st = wlg::launch_pre_batch(static_cast<const PreDesc*>(ctx->pre_desc.p), n, threads, smem,
+                             static_cast<int8_t*>(ctx->J8.p), static_cast<uint8_t*>(ctx->seen.p),
+                             static_cast<int8_t*>(ctx->found.p), static_cast<int*>(ctx->fflag.p), ctx->stream);
+  if (st != WLG_OK) return fail(ctx, st, "pre-run launch failed");
+  ++ctx->launches;
+  cudaEventRecord(ctx->ev[1], ctx->stream);
+  std::vector<int8_t> J8(static_cast<size_t>(oJ)), found(static_cast<size_t>(oF));
+  std::vector<uint8_t> seen(static_cast<size_t>(oS));
+  std::vector<int> fflag(static_cast<size_t>(oG));
+  download(ctx, ctx->J8, J8);
+  download(ctx, ctx->seen, seen);
+  download(ctx, ctx->found, found);
+  download(ctx, ctx->fflag, fflag);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, WLG_ERR_CUDA, "pre-run failed");
+  cudaEventElapsedTime(&ctx->t_pre, ctx->ev[0], ctx->ev[1]);
+
+  // ---------------- hand-off (file_io.cpp:558-659, mainrun.cu:79-113)
+  const auto t0 = clock::now();
+  std::vector<uint32_t> Jw, latw, maskw;
+  std::vector<int> win;
+  long long o_out = 0;
+  prep.starts.assign(static_cast<size_t>(n), {});
+  prep.ends.assign(static_cast<size_t>(n), {});
+  for (int p = 0; p < n; ++p) {
+    const wlg_problem& q = probs[p];
+    const PreDesc& a = pd[p];
+    const int N = a.N;
+    const uint8_t* h = seen.data() + a.off_seen;
+    int first = -1, last = -1;
+    for (int i = 0; i <= 4 * N; ++i)
+      if (h[i] == 1) {
+        if (first < 0) first = i;
+        last = i;
+      }
+    if (first < 0) {
+      results[p].status = WLG_ERR_NO_LATTICE;
+      continue;
+    }
+    const int e_lo = -2 * N + first, e_hi = -2 * N + last;
+    std::vector<int> ws, we;
+    const wlg_status wst = wlg::make_windows(e_lo, e_hi, q.intervals, q.overlap, ws, we);
+    if (wst != WLG_OK) {
+      results[p].status = wst;
+      continue;
+    }
+    prep.starts[p] = ws;
+    prep.ends[p] = we;
+    // energy step of the lattice: 4 when every site has an even number of
+    // bonds (periodic, or open 2x2), else 2; checked against the spectrum
+    int g = (q.boundary == 0 || (q.X == 2 && q.Y == 2)) ? 4 : 2;
+    for (int i = first; i <= last; ++i)
+      if (h[i] == 1 && (i - first) % g != 0) g = ((i - first) % 2 == 0) ? 2 : 1;
+    const int lg = g == 4 ? 2 : (g == 2 ? 1 : 0);
+    // start lattices: lowest-energy stored lattice inside each window
+    std::map<int, int> by_energy;
+    for (int k = 0; k < a.n_int; ++k)
+      if (fflag[a.off_fflag + k] != 0) by_energy.emplace(fflag[a.off_fflag + a.n_int + k], k);
+    const int nwL = (N + 31) / 32;
+    std::vector<int> pick(static_cast<size_t>(q.intervals), -1), E0(static_cast<size_t>(q.intervals));
+    bool ok = true;
+    for (int b = 0; b < q.intervals && ok; ++b) {
+      for (const auto& [en, k] : by_energy)
+        if (en >= ws[b] && en <= we[b]) {
+          pick[b] = k;
+          E0[b] = en;
+          break;
+        }
+      ok = pick[b] >= 0;
+    }
+    if (!ok) {
+      results[p].status = WLG_ERR_NO_LATTICE;
+      continue;
+    }
+    MainDesc d{};
+    d.X = q.X;
+    d.Y = q.Y;
+    d.N = N;
+    d.boundary = q.boundary;
+    d.I = q.intervals;
+    d.W = q.walkers_per_interval;
+    d.nwalk = d.I * d.W;
+    d.team = round32(d.nwalk);
+    d.e_min = e_lo;
+    d.e_max = e_hi;
+    d.lg = lg;
+    d.n_iter = q.iterations;
+    d.exch_every = q.exchange_every;
+    d.exch_mode = q.exchange_mode;
+    d.parity_base = q.global_parity ? static_cast<int>((static_cast<long long>(q.sample) * q.intervals) & 1) : 0;
+    d.alpha = q.alpha;
+    d.beta = q.beta;
+    d.loop_lim = std::exp(q.beta);
+    d.key_wl = static_cast<uint32_t>(wlg::key_u32(q.seed, static_cast<uint64_t>(q.sample)));
+    d.key_ex = wlg::key_i32(q.seed, static_cast<uint64_t>(q.sample));
+    d.site_magic = static_cast<uint32_t>(((1u << 20) + q.Y - 1) / q.Y);
+    for (int site = 0; site < N; ++site)
+      if (static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20) != site / q.Y) ok = false;
+    if (!ok) return fail(ctx, WLG_ERR_INVALID, "lattice too large for the site division");
+    d.site_scale = (N - 1 + 0.999999);
+    d.site_scale_f = static_cast<float>(d.site_scale);
+    d.site_eps = static_cast<float>(N) * 0x1p-21f;
+    d.max_outer = q.max_outer;
+    d.nwL = nwL;
+    const int nbins = (e_hi - e_lo) / g + 1;
+    d.nwM = (nbins + 31) / 32;
+    // windows: start, end, compact base (first energy >= start on the lattice
+    // of reachable energies), compact length, start energy
+    int L = 1;
+    std::vector<int> base(static_cast<size_t>(d.I)), len(static_cast<size_t>(d.I));
+    for (int b = 0; b < d.I; ++b) {
+      const int r = ((e_lo - ws[b]) % g + g) % g;
+      base[b] = ws[b] + r;
+      len[b] = base[b] <= we[b] ? (we[b] - base[b]) / g + 1 : 0;
+      L = std::max(L, len[b]);
+    }
+    d.L = L;
+    d.off_J = static_cast<long long>(Jw.size());
+    for (int half = 0; half < 2; ++half)
+      for (int wd = 0; wd < nwL; ++wd) {
+        uint32_t v = 0;
+        for (int bit = 0; bit < 32; ++bit) {
+          const int q2 = wd * 32 + bit;
+          if (q2 < N && J8[a.off_J + half * N + q2] == -1) v |= 1u << bit;
+        }
+        Jw.push_back(v);
+      }
+    d.off_lat = static_cast<long long>(latw.size());
+    for (int b = 0; b < d.I; ++b) {
+      const int8_t* src = found.data() + a.off_found + static_cast<long long>(pick[b]) * N;
+      if (wlg::energy_host(src, J8.data() + a.off_J, q.X, q.Y, q.boundary) != E0[b])
+        return fail(ctx, WLG_ERR_ENERGY_RANGE, "stored lattice energy mismatch");
+      for (int wd = 0; wd < nwL; ++wd) {
+        uint32_t v = 0;
+        for (int bit = 0; bit < 32; ++bit) {
+          const int q2 = wd * 32 + bit;
+          if (q2 < N && src[q2] == -1) v |= 1u << bit;
+        }
+        latw.push_back(v);
+      }
+    }
+    d.off_win = static_cast<long long>(win.size());
+    win.insert(win.end(), ws.begin(), ws.end());
+    win.insert(win.end(), we.begin(), we.end());
+    win.insert(win.end(), base.begin(), base.end());
+    win.insert(win.end(), len.begin(), len.end());
+    win.insert(win.end(), E0.begin(), E0.end());
+    d.off_mask = static_cast<long long>(maskw.size());
+    for (int wd = 0; wd < d.nwM; ++wd) {
+      uint32_t v = 0;
+      for (int bit = 0; bit < 32; ++bit) {
+        const int c = wd * 32 + bit;
+        if (c < nbins && h[first + c * g] == 1) v |= 1u << bit;
+      }
+      maskw.push_back(v);
+    }
+    d.off_out = o_out;
+    o_out += static_cast<long long>(d.I) * d.L;
+    d.off_dump = -1;
+    prep.main.push_back(d);
+    prep.main_problem.push_back(p);
+    prep.lg.push_back(lg);
+  }
+  ctx->t_handoff = std::chrono::duration<double, std::milli>(clock::now() - t0).count();
+
+  // ---------------- main run: one persistent launch per (lattice storage, team size)
+  const int m = static_cast<int>(prep.main.size());
+  mres.assign(static_cast<size_t>(m), MainResult{});
+  out_host.assign(static_cast<size_t>(o_out), 0.0);
+  win_host = win;
+  if (m == 0) {
+    ctx->t_main = 0;
+    return WLG_OK;
+  }
+  std::map<std::pair<int, int>, std::vector<int>> groups;
+  for (int i = 0; i < m; ++i) groups[{prep.main[i].N <= 64 ? 1 : 0, prep.main[i].team}].push_back(i);
+  std::vector<int> order;
+  std::vector<std::tuple<bool, int, int, int, int, int>> launches;  // reg, team, bytes, per_cta, first, count
+  for (const auto& [key, idx] : groups) {
+    const bool reg = key.first == 1;
+    const int team = key.second;
+    int bytes = 0;
+    for (int i : idx) {
+      const MainDesc& d = prep.main[i];
+      bytes = std::max(bytes, wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, reg).bytes + 16);
+    }
+    bytes = wlg::align16(bytes);
+    if (bytes > 227 * 1024) return fail(ctx, WLG_ERR_INVALID, "problem state exceeds shared memory");
+    int per_cta = team <= 256 ? 256 / team : 1;
+    per_cta = std::min(per_cta, (227 * 1024) / bytes);
+    if (team > 32) per_cta = std::min(per_cta, 15);
+    per_cta = std::max(per_cta, 1);
+    launches.emplace_back(reg, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()));
+    order.insert(order.end(), idx.begin(), idx.end());
+  }
+  if ((st = upload(ctx, ctx->main_desc, prep.main)) != WLG_OK) return st;
+  if ((st = upload(ctx, ctx->order, order)) != WLG_OK) return st;
+  if ((st = upload(ctx, ctx->Jw, Jw)) != WLG_OK) return st;
+  if ((st = upload(ctx, ctx->latw, latw)) != WLG_OK) return st;
+  if ((st = upload(ctx, ctx->win, win)) != WLG_OK) return st;
+  if ((st = upload(ctx, ctx->mask, maskw)) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->out, static_cast<size_t>(o_out) * sizeof(double))) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->res, static_cast<size_t>(m) * sizeof(MainResult))) != WLG_OK) return st;
+  if ((st = grow(ctx, ctx->next, launches.size() * sizeof(int))) != WLG_OK) return st;
+  cudaMemsetAsync(ctx->next.p, 0, launches.size() * sizeof(int), ctx->stream);
+  cudaEventRecord(ctx->ev[2], ctx->stream);
+  for (size_t g = 0; g < launches.size(); ++g) {
+    const auto [reg, team, bytes, per_cta, first, count] = launches[g];
+    const int cap = wlg::main_batch_capacity(reg, team * per_cta, bytes * per_cta);
+    if (cap <= 0) return fail(ctx, WLG_ERR_CUDA, "main-run configuration does not fit an SM");
+    const int grid = std::min(cap, (count + per_cta - 1) / per_cta);
+    st = wlg::launch_main_batch(reg, static_cast<const MainDesc*>(ctx->main_desc.p),
+                                static_cast<const int*>(ctx->order.p) + first, count, team, bytes, per_cta, grid,
+                                static_cast<int*>(ctx->next.p) + g, static_cast<const uint32_t*>(ctx->Jw.p),
+                                static_cast<const uint32_t*>(ctx->latw.p), static_cast<const int*>(ctx->win.p),
+                                static_cast<const uint32_t*>(ctx->mask.p), static_cast<double*>(ctx->out.p),
+                                static_cast<MainResult*>(ctx->res.p), nullptr, ctx->stream);
+    if (st != WLG_OK) return fail(ctx, st, "main-run launch failed");
+    ++ctx->launches;
+  }
+  cudaEventRecord(ctx->ev[3], ctx->stream);
+  download(ctx, ctx->res, mres);
+  download(ctx, ctx->out, out_host);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, WLG_ERR_CUDA, "main run failed");
+  cudaEventElapsedTime(&ctx->t_main, ctx->ev[2], ctx->ev[3]);
+  for (int i = 0; i < m; ++i) {
+    wlg_result& r = results[prep.main_problem[i]];
+    r.status = mres[i].status;
+    r.new_energy = mres[i].new_energy;
+    r.outer_iterations = mres[i].outer;
+    r.flips = mres[i].flips;
+  }
+  return WLG_OK;
+}
+
+// Dense walker-0 log g of window b (zeros where the lattice cannot reach).
+void dense_window(const MainDesc& d, const std::vector<double>& out, const std::vector<int>& win, int b,
+                  std::vector<double>& dense)
+{
+  const int s = win[d.off_win + b], e = win[d.off_win + d.I + b];
+  const int base = win[d.off_win + 2 * d.I + b], len = win[d.off_win + 3 * d.I + b];
+  dense.assign(static_cast<size_t>(e - s + 1), 0.0);
+  for (int c = 0; c < len; ++c) dense[base + (c << d.lg) - s] = out[d.off_out + static_cast<long long>(b) * d.L + c];
+}
+
+}  // namespace
+
+extern "C" {
+
+wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context** out)
+{
+  if (out == nullptr) return WLG_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return WLG_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return WLG_ERR_CUDA;
+  auto* ctx = new wlg_context();
+  ctx->device = device;
+  ctx->budget = mem_budget_bytes;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return WLG_ERR_CUDA;
+  }
+  for (auto& e : ctx->ev) cudaEventCreate(&e);
+  *out = ctx;
+  return WLG_OK;
+}
+
+wlg_status wlg_context_destroy(wlg_context* ctx)
+{
+  if (ctx == nullptr) return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (DevBuf* b : {&ctx->pre_desc, &ctx->J8, &ctx->seen, &ctx->found, &ctx->fflag, &ctx->main_desc, &ctx->order,
+                    &ctx->next, &ctx->Jw, &ctx->latw, &ctx->win, &ctx->mask, &ctx->out, &ctx->res, &ctx->dump})
+    if (b->p != nullptr) cudaFree(b->p);
+  for (auto& e : ctx->ev) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return WLG_OK;
+}
+
+const char* wlg_context_last_error(const wlg_context* ctx) { return ctx == nullptr ? "" : ctx->err.c_str(); }
+
+wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* win_start,
+                         int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset)
+{
+  if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<MainResult> mres;
+  Prepared prep;
+  std::vector<double> out;
+  std::vector<int> win;
+  wlg_status st = run_batch(ctx, problems, n, results, mres, prep, out, win);
+  if (st != WLG_OK) return st;
+  long long pos = 0;
+  std::vector<int> slot(static_cast<size_t>(n), -1);
+  for (size_t i = 0; i < prep.main.size(); ++i) slot[prep.main_problem[i]] = static_cast<int>(i);
+  long long wpos = 0;
+  for (int p = 0; p < n; ++p) {
+    if (raw_offset != nullptr) raw_offset[p] = pos;
+    const int I = problems[p].intervals;
+    for (int b = 0; b < I; ++b) {
+      const bool have = !prep.starts[p].empty();
+      if (win_start != nullptr) win_start[wpos + b] = have ? prep.starts[p][b] : 0;
+      if (win_end != nullptr) win_end[wpos + b] = have ? prep.ends[p][b] : -1;
+    }
+    wpos += I;
+    if (slot[p] < 0) continue;
+    const MainDesc& d = prep.main[slot[p]];
+    std::vector<double> dense;
+    for (int b = 0; b < d.I; ++b) {
+      dense_window(d, out, win, b, dense);
+      if (pos + static_cast<long long>(dense.size()) > raw_capacity) return fail(ctx, WLG_ERR_CAPACITY, "raw output");
+      if (raw_log_g != nullptr) std::memcpy(raw_log_g + pos, dense.data(), dense.size() * sizeof(double));
+      pos += static_cast<long long>(dense.size());
+    }
+  }
+  return WLG_OK;
+}
+
+wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* energies,
+                     double* log_g, long long capacity)
+{
+  if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<MainResult> mres;
+  Prepared prep;
+  std::vector<double> out;
+  std::vector<int> win;
+  wlg_status st = run_batch(ctx, problems, n, results, mres, prep, out, win);
+  if (st != WLG_OK) return st;
+  const auto t0 = std::chrono::steady_clock::now();
+  long long pos = 0;
+  std::vector<double> dense;
+  for (size_t i = 0; i < prep.main.size(); ++i) {
+    const int p = prep.main_problem[i];
+    wlg_result& r = results[p];
+    r.offset = pos;
+    r.n_energies = 0;
+    if (r.status != WLG_OK) continue;
+    const MainDesc& d = prep.main[i];
+    std::vector<wlg::Curve> curves(static_cast<size_t>(d.I));
+    for (int b = 0; b < d.I; ++b) {
+      dense_window(d, out, win, b, dense);
+      const int s = win[d.off_win + b];
+      for (size_t k = 0; k < dense.size(); ++k)
+        if (dense[k] != 0) curves[b].emplace(s + static_cast<int>(k), dense[k]);
+    }
+    std::vector<std::pair<int, double>> res;
+    const wlg_status sst = wlg::stitch_windows(std::move(curves), d.X, d.Y, res);
+    if (sst != WLG_OK) {
+      r.status = sst;
+      continue;
+    }
+    if (pos + static_cast<long long>(res.size()) > capacity) return fail(ctx, WLG_ERR_CAPACITY, "result arrays");
+    for (size_t k = 0; k < res.size(); ++k) {
+      energies[pos + static_cast<long long>(k)] = res[k].first;
+      log_g[pos + static_cast<long long>(k)] = res[k].second;
+    }
+    r.n_energies = static_cast<int>(res.size());
+    pos += static_cast<long long>(res.size());
+  }
+  ctx->t_stitch = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return WLG_OK;
+}
+
+wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)
+{
+  if (ctx == nullptr || out == nullptr) return WLG_ERR_INVALID;
+  out->pre_ms = ctx->t_pre;
+  out->handoff_ms = ctx->t_handoff;
+  out->main_ms = ctx->t_main;
+  out->stitch_ms = ctx->t_stitch;
+  out->h2d_bytes = ctx->h2d;
+  out->d2h_bytes = ctx->d2h;
+  out->kernel_launches = ctx->launches;
+  return WLG_OK;
+}
+
+wlg_status wlg_class_log_probs(const int* energies, const double* log_g, const long long* offset, const int* count,
+                               int n_classes, double prob, double* log_z, double* log_probs)
+{
+  if (n_classes <= 0 || prob <= 0 || prob >= 1 || energies == nullptr || log_g == nullptr) return WLG_ERR_INVALID;
+  const double beta_n = 0.5 * std::log((1.0 - prob) / prob);
+  std::vector<double> lz(static_cast<size_t>(n_classes));
+  for (int c = 0; c < n_classes; ++c) {
+    if (count[c] <= 0) return WLG_ERR_INVALID;
+    double mx = -std::numeric_limits<double>::infinity();
+    for (int i = 0; i < count[c]; ++i) {
+      const long long k = offset[c] + i;
+      mx = std::max(mx, log_g[k] - beta_n * energies[k]);
+    }
+    double s = 0;
+    for (int i = 0; i < count[c]; ++i) {
+      const long long k = offset[c] + i;
+      s += std::exp(log_g[k] - beta_n * energies[k] - mx);
+    }
+    lz[c] = mx + std::log(s);
+  }
+  double mx = *std::max_element(lz.begin(), lz.end());
+  double s = 0;
+  for (double v : lz) s += std::exp(v - mx);
+  const double lse = mx + std::log(s);
+  for (int c = 0; c < n_classes; ++c) {
+    if (log_z) log_z[c] = lz[c];
+    if (log_probs) log_probs[c] = lz[c] - lse;
+  }
+  return WLG_OK;
+}
+
+}  // extern "C"

@@ -17,49 +17,13 @@
 
 #include "../../include/wlg.h"
 #include "wlg_internal.h"
+#include "wlg_lattice.cuh"
 #include "wlg_rng.cuh"
 
 namespace wlg {
 namespace {
 
 constexpr int kThreads = 128;
-
-// ------------------------------------------------------ spin-flip proposal --
-
-struct Move {
-  int new_energy;
-  int site;
-};
-
-// wl.cu:52-208: one uniform picks the site (double arithmetic exactly as the
-// reference), dE from the four neighbours; open boundaries drop the bonds
-// that would wrap.
-__device__ __forceinline__ Move propose(Stream& rng, const int8_t* __restrict__ s, const int8_t* __restrict__ J,
-                                        int E, int X, int Y, double site_scale, int boundary)
-{
-  const int N = X * Y;
-  double u = rng.uniform();
-  u *= site_scale;
-  const int site = static_cast<int>(trunc(u));
-  const int i = site / Y;
-  const int j = site - i * Y;
-  const int ip = (i + 1 < X) ? i + 1 : 0;
-  const int im = (i - 1 >= 0) ? i - 1 : X - 1;
-  const int jp = (j + 1 < Y) ? j + 1 : 0;
-  const int jm = (j - 1 >= 0) ? j - 1 : Y - 1;
-  int up = s[im * Y + j] * J[N + im * Y + j];
-  int left = s[i * Y + jm] * J[i * Y + jm];
-  int down = s[ip * Y + j] * J[N + i * Y + j];
-  int right = s[i * Y + jp] * J[i * Y + j];
-  if (boundary == 1) {
-    up = (i == 0) ? 0 : up;
-    down = (i + 1 == X) ? 0 : down;
-    right = (j == Y - 1) ? 0 : right;
-    left = (j == 0) ? 0 : left;
-  }
-  const int dE = -2 * s[site] * (up + left + down + right);
-  return {E - dE, site};
-}
 
 // -------------------------------------------------------------- disorder ----
 
@@ -112,24 +76,8 @@ __global__ void k_calc_energy(int boundary, int* __restrict__ E, const int8_t* _
 {
   const size_t t = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= num_lattices) return;
-  const int N = X * Y;
-  const int8_t* s = lat + off_lat[t];
-  const int8_t* Jk = J + (t / static_cast<size_t>(wpi)) * 2 * N;
-  int acc = 0;
-  for (int i = 0; i < X; ++i) {
-    const int im = (i - 1 >= 0) ? i - 1 : X - 1;
-    for (int j = 0; j < Y; ++j) {
-      const int jm = (j - 1 >= 0) ? j - 1 : Y - 1;
-      int up = s[im * Y + j] * Jk[N + im * Y + j];
-      int left = s[i * Y + jm] * Jk[i * Y + jm];
-      if (boundary == 1) {
-        up = (i == 0) ? 0 : up;
-        left = (j == 0) ? 0 : left;
-      }
-      acc += s[i * Y + j] * (up + left);
-    }
-  }
-  E[t] = -acc;
+  const size_t N = static_cast<size_t>(X) * Y;
+  E[t] = energy_i8(lat + off_lat[t], J + (t / static_cast<size_t>(wpi)) * 2 * N, X, Y, boundary);
 }
 
 // --------------------------------------------------------------- pre-run ----
@@ -179,7 +127,7 @@ __global__ void k_prerun(int* __restrict__ E, int* __restrict__ flag_found, int8
     int hit = -1;
     bool acc = false;
     if (live && ok) {
-      const Move m = propose(rng, s, Jk, energy, X, Y, site_scale, boundary);
+      const Move m = propose_i8(rng, s, Jk, energy, X, Y, site_scale, boundary);
       if (m.new_energy > E_max || m.new_energy < E_min) {  // wl.cu:522-529: the walker stops
         energy = m.new_energy;                               // and keeps the offending energy
         ok = false;
@@ -258,7 +206,7 @@ __global__ void k_wang_landau(int8_t* __restrict__ lat, const int8_t* __restrict
   int energy = E[t];
   int flag = 0;
   for (int it = 0; it < n_iter; ++it) {
-    const Move m = propose(rng, s, Jk, energy, X, Y, site_scale, boundary);
+    const Move m = propose_i8(rng, s, Jk, energy, X, Y, site_scale, boundary);
     // wl.cu:1091-1104; an energy outside the sample's spectrum range counts
     // as new too (the reference reads the mask out of bounds there).
     if (m.new_energy < e_first || m.new_energy > e_last || mask[m.new_energy] != 1) {

@@ -1,0 +1,155 @@
+"""The batched engine (one pre-run CTA and one persistent main-run team per
+problem) against the oracle's restatement of prerun.cu + mainrun.cu.
+
+Every problem's trajectory is deterministic given (seed, sample), so the
+walker-0 log g of every window must equal the oracle's bit for bit, and the
+stitched, normalised result must equal the oracle's stitching of it.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_run(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc,
+               xmode, gpar):
+    N = X * Y
+    seen = np.zeros(R * (4 * N + 1), np.uint8)
+    J = np.zeros(R * 2 * N, np.int8)
+    flat = np.zeros(R * pre_i * N, np.int8)
+    flag = np.zeros(R * pre_i, np.int32)
+    en = np.zeros(R * pre_i, np.int32)
+    L = O.lib()
+    L.orc_prerun(X, Y, boundary, C.c_float(prob), cls.encode(), seed, R, pre_w, pre_i, pre_n, O.ptr(seen), O.ptr(J),
+                 O.ptr(flat), O.ptr(flag), O.ptr(en))
+    start = np.zeros(R * I, np.int32)
+    end = np.zeros(R * I, np.int32)
+    off_hist = np.zeros(R * I * W, np.int32)
+    n_log = C.c_longlong(0)
+    ci = np.zeros(R, np.int32)
+    outer = C.c_longlong(0)
+    flips = C.c_longlong(0)
+    args = (X, Y, boundary, R, I, W, C.c_float(overlap), alpha, beta, n_iter, xc, xmode, gpar, seed, 0, O.ptr(seen),
+            O.ptr(J), O.ptr(flat), O.ptr(flag), O.ptr(en), pre_i, O.ptr(start), O.ptr(end), O.ptr(off_hist))
+    st = L.orc_mainrun(*args, None, C.byref(n_log), O.ptr(ci), C.byref(outer), C.byref(flips))
+    logG = np.zeros(max(n_log.value, 1), np.float64)
+    st = L.orc_mainrun(*args, O.ptr(logG), C.byref(n_log), O.ptr(ci), C.byref(outer), C.byref(flips))
+    return dict(status=st, start=start, end=end, off_hist=off_hist, logG=logG, cond=ci, outer=outer.value,
+                flips=flips.value)
+
+
+CONFIGS = [
+    # X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc, xmode, gpar
+    (4, 4, 0, 0.04, "i", 12345, 3, 32, 8, 2000, 10, 3, 0.25, 0.8, 0.001, 1000, 20, 1, 0),
+    (4, 4, 0, 0.10, "c", 7, 4, 32, 8, 2000, 4, 3, 0.25, 0.8, 0.01, 500, 1, 0, 1),
+    (5, 4, 1, 0.20, "h", 99, 3, 32, 9, 3000, 5, 2, 0.5, 0.8, 0.005, 400, 3, 1, 0),
+    (6, 6, 0, 0.04, "v", 12345, 2, 128, 32, 2000, 10, 3, 0.25, 0.8, 0.01, 1000, 20, 1, 0),
+    (5, 5, 1, 0.20, "i", 31337, 2, 64, 16, 3000, 7, 3, 0.25, 0.8, 0.01, 800, 2, 1, 1),
+    (9, 8, 0, 0.08, "i", 5, 1, 64, 16, 3000, 8, 2, 0.25, 0.7, 0.05, 1500, 4, 1, 0),
+]
+
+
+@pytest.mark.parametrize("cfg", CONFIGS, ids=[f"{c[0]}x{c[1]}b{c[2]}{c[4]}" for c in CONFIGS])
+def test_engine_full_run_bit_exact(cuda, cfg):
+    import qec_pf_wang_landau_gb300 as wlg
+    (X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc, xmode,
+     gpar) = cfg
+    ref = oracle_run(*cfg)
+    assert ref["status"] == 0
+    probs = [wlg.problem(X, Y, boundary=boundary, prob=prob, error_class=cls, seed=seed, sample=k,
+                         pre_walkers=pre_w, pre_intervals=pre_i, pre_iterations=pre_n, intervals=I,
+                         walkers_per_interval=W, overlap=overlap, alpha=alpha, beta=beta, iterations=n_iter,
+                         exchange_every=xc, exchange_mode=xmode, global_parity=gpar) for k in range(R)]
+    ctx = wlg.Context(0)
+    out = ctx.solve_raw(probs)
+    total_flips = 0
+    for k, (res, s, e, wins) in enumerate(out):
+        assert res.status == 0, (k, res.status, res.new_energy)
+        total_flips += res.flips
+        assert np.array_equal(s, ref["start"][k * I:(k + 1) * I])
+        assert np.array_equal(e, ref["end"][k * I:(k + 1) * I])
+        for b in range(I):
+            o = ref["off_hist"][(k * I + b) * W]
+            want = ref["logG"][o:o + (e[b] - s[b] + 1)]
+            assert np.array_equal(wins[b], want), f"sample {k} window {b}: max |d| {np.abs(wins[b] - want).max()}"
+    assert total_flips == ref["flips"]
+
+    # stitched result == the oracle's stitching of the same windows
+    solved = ctx.solve(probs)
+    for k, (res, E, G) in enumerate(solved):
+        o = ref["off_hist"][k * I * W]
+        sl = ref["logG"][o:]
+        Eo = np.zeros(4 * X * Y + 1, np.int32)
+        Go = np.zeros(4 * X * Y + 1, np.float64)
+        nout = C.c_int(0)
+        rc = O.lib().orc_stitch(O.ptr(np.ascontiguousarray(sl)), O.ptr(ref["start"][k * I:]),
+                                O.ptr(ref["end"][k * I:]), I, W, X, Y, O.ptr(Eo), O.ptr(Go), len(Eo),
+                                C.byref(nout))
+        assert rc == 0
+        assert np.array_equal(E, Eo[:nout.value])
+        assert np.array_equal(G, Go[:nout.value])
+        lse = np.logaddexp.reduce(G)
+        assert abs(lse - X * Y * np.log(2)) < 1e-9
+
+
+def test_engine_heterogeneous_batch_equals_separate_runs(cuda):
+    """Problems of different shapes in one batch give the same results as alone."""
+    import qec_pf_wang_landau_gb300 as wlg
+    mk = lambda X, Y, b, k, c: wlg.problem(X, Y, boundary=b, prob=0.08, error_class=c, seed=4242, sample=k,
+                                           pre_walkers=64, pre_intervals=16, pre_iterations=2000, intervals=6,
+                                           walkers_per_interval=4, beta=0.02, iterations=600, exchange_every=2)
+    batch = [mk(4, 4, 0, 0, "i"), mk(6, 6, 0, 1, "v"), mk(5, 7, 1, 2, "h"), mk(8, 8, 0, 3, "c"), mk(9, 9, 1, 4, "i")]
+    ctx = wlg.Context(0)
+    together = ctx.solve(batch)
+    for p, (r, E, G) in zip(batch, together):
+        (r1, E1, G1), = ctx.solve([p])
+        assert r.status == r1.status == 0
+        assert r.flips == r1.flips and r.outer_iterations == r1.outer_iterations
+        assert np.array_equal(E, E1) and np.array_equal(G, G1)
+
+
+def test_engine_4x4_log_g_against_exact_enumeration(cuda):
+    """Config 1 (4x4 periodic, p=0.04, seed 12345, class i): the normalised log g
+    against exact FP64 enumeration of all 2^16 states."""
+    import qec_pf_wang_landau_gb300 as wlg
+    p = wlg.problem(4, 4, prob=0.04, error_class="i", seed=12345, sample=0, pre_walkers=32, pre_intervals=8,
+                    pre_iterations=1000, intervals=10, walkers_per_interval=3, overlap=0.25, alpha=0.8, beta=1e-3,
+                    iterations=1000, exchange_every=20)
+    ctx = wlg.Context(0)
+    (r, E, G), = ctx.solve([p])
+    assert r.status == 0
+    J = O.init_interactions(4, 4, 1, 12345, 0.04, "i")
+    counts = O.exact_counts(J, 4, 4, 0)
+    exact_E = np.nonzero(counts)[0] - 32
+    assert set(E.tolist()) == set(exact_E.tolist())
+    exact = np.log(counts[E + 32])
+    err = G - exact
+    assert np.sqrt(np.mean(err ** 2)) < 0.25
+    assert np.abs(err).max() < 0.6
+
+
+def test_class_log_probs_normalised(cuda):
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = [wlg.problem(4, 4, prob=0.1, error_class=c, seed=77, sample=0, pre_walkers=32, pre_intervals=8,
+                         pre_iterations=2000, intervals=4, walkers_per_interval=3, beta=0.01, iterations=500)
+             for c in "ivhc"]
+    ctx = wlg.Context(0)
+    out = ctx.solve(probs)
+    assert all(r.status == 0 for r, _, _ in out)
+    lz, lp = wlg.class_log_probs([(E, G) for _, E, G in out], 0.1)
+    assert abs(np.logaddexp.reduce(lp)) < 1e-12
+    # exact class probabilities from enumeration agree to WL accuracy
+    exact = []
+    for c in "ivhc":
+        J = O.init_interactions(4, 4, 1, 77, 0.1, c)
+        cnt = O.exact_counts(J, 4, 4, 0)
+        Ee = np.nonzero(cnt)[0] - 32
+        bn = 0.5 * np.log(0.9 / 0.1)
+        exact.append(np.logaddexp.reduce(np.log(cnt[Ee + 32]) - bn * Ee))
+    exact = np.array(exact) - np.logaddexp.reduce(exact)
+    assert np.argmax(lp) == np.argmax(exact)
+    assert np.abs(np.exp(lp) - np.exp(exact)).max() < 0.05

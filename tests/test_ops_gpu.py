@@ -87,14 +87,20 @@ def test_prerun_acceptance_exp_decisions_match(cuda, probe):
     hl = np.zeros_like(x)
     O.lib().orc_exp_log(O.ptr(np.ascontiguousarray(x)), O.ptr(he), O.ptr(hl), len(x))
     ge = de.cpu().numpy()
+    u_min = 2.0 ** -33  # the smallest uniform a draw can give
+    n_diff = 0
     for a, b in zip(ge, he):
         lo, hi = min(a, b), max(a, b)
-        if lo == hi or hi <= 0:
+        if lo == hi or hi < u_min:
             continue
-        # no float strictly inside [lo, hi) may separate the decisions
-        f = np.float32(lo)
-        f = f if f >= lo else np.nextafter(f, np.float32(np.inf))
+        n_diff += 1
+        # no reachable float uniform u may satisfy lo <= u < hi
+        if lo > 1.0:
+            continue
+        f = np.float32(max(lo, u_min))
+        f = f if float(f) >= lo else np.nextafter(f, np.float32(np.inf))
         assert not (lo <= float(f) < hi), (a, b)
+    assert n_diff < len(x) // 10
 
 
 @pytest.mark.parametrize("X,Y,R,seed,prob", [(4, 4, 3, 1, 0.15), (6, 6, 5, 12345, 0.04), (7, 5, 4, -17, 0.5),
@@ -144,11 +150,11 @@ def test_calc_energy_known_answers(cuda):
     lat = np.array([1, 1, -1, 1, -1, -1, 1, -1, 1, -1, 1, -1, -1, -1, -1, -1], np.int8)
     J = np.array([1, -1, 1, 1, 1, 1, 1, 1, -1, 1, 1, -1, 1, 1, 1, 1, 1, 1, -1, 1, 1, 1, 1, 1, -1, 1, 1, 1, 1, 1, 1,
                   1], np.int8)
+    dlat, dJ = torch.from_numpy(lat).cuda(), torch.from_numpy(J).cuda()  # keep the buffers alive
+    doff = torch.zeros(1, dtype=torch.int32, device="cuda")
     for boundary, want in ((0, -6), (1, -4)):
         dE = torch.zeros(1, dtype=torch.int32, device="cuda")
-        wlg.call("wlg_calc_energy", boundary, _dptr(dE), _dptr(torch.from_numpy(lat).cuda()),
-                 _dptr(torch.from_numpy(J).cuda()), _dptr(torch.zeros(1, dtype=torch.int32, device="cuda")), 4, 4, 1,
-                 1, None)
+        wlg.call("wlg_calc_energy", boundary, _dptr(dE), _dptr(dlat), _dptr(dJ), _dptr(doff), 4, 4, 1, 1, None)
         assert int(dE.item()) == want
     ones = torch.ones(10 * 16, dtype=torch.int8, device="cuda")
     Jones = torch.ones(2 * 32, dtype=torch.int8, device="cuda")

@@ -1,0 +1,264 @@
+"""CPU tests: the oracle pinned against the reference's own known-answer
+tests (test/*.cpp, test/*.cu and test/integration_*.py), and its internal
+consistency (transfer matrix vs enumeration, round trips)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from tests.helpers import mainrun_state, o_average, o_check_histogram, o_exchange, prerun_outputs
+
+
+# ----------------------------------------------------------- test_interval.cpp
+
+def test_interval_typical_8x8():
+    """test_interval.cpp:12-38."""
+    s, e, tot, ln = O.interval_results(-128, 128, 16, 8, 0.25)
+    assert ln == 54
+    assert len(s) == 16 and len(e) == 16
+    assert e[15] == 128 and s[0] == -128 and s[15] == 67
+    assert tot == 62 * 8 + 54 * 8 * 15
+
+
+def test_interval_empty_window_throws():
+    with pytest.raises(ValueError, match="empty"):
+        O.interval_results(-16, 16, 64, 8, 1.0)
+
+
+def test_interval_overlap_out_of_bounds_throws():
+    with pytest.raises(ValueError, match="Overlap"):
+        O.interval_results(-16, 16, 64, 8, 1.1)
+
+
+def test_interval_prerun_bins():
+    """prerun.cu:23-25: coarse bins of [-2N, 2N] with overlap 1 (C2: 6x6, 32 bins)."""
+    s, e, _, ln = O.interval_results(-72, 72, 32, 1, 1.0)
+    assert ln == 145 // 32 and s[1] - s[0] == ln and e[-1] == 72
+
+
+# ---------------------------------------------------------- test_calc_energy.cu
+
+LAT = np.array([1, 1, -1, 1, -1, -1, 1, -1, 1, -1, 1, -1, -1, -1, -1, -1], np.int8)
+JJ = np.array([1, -1, 1, 1, 1, 1, 1, 1, -1, 1, 1, -1, 1, 1, 1, 1, 1, 1, -1, 1, 1, 1, 1, 1, -1, 1, 1, 1, 1, 1, 1, 1],
+              np.int8)
+
+
+def test_energy_known_answers():
+    off = np.zeros(1, np.int32)
+    assert O.calc_energy(0, LAT, JJ, off, 4, 4, 1, 1)[0] == -6
+    assert O.calc_energy(1, LAT, JJ, off, 4, 4, 1, 1)[0] == -4
+    ones = np.ones(10 * 16, np.int8)
+    J1 = np.ones(2 * 32, np.int8)
+    offs = (np.arange(10) * 16).astype(np.int32)
+    assert (O.calc_energy(0, ones, J1, offs, 4, 4, 10, 5) == -32).all()
+    assert (O.calc_energy(1, ones, J1, offs, 4, 4, 10, 5) == -32 + 8).all()
+
+
+# ---------------------------------------------------- test_init_interactions.cu
+
+def test_error_chain_layouts():
+    """test_init_interactions.cu:48-188 (p = 0, 4x4, 2 samples)."""
+    h = O.init_interactions(4, 4, 2, 1, 0.0, "h").reshape(2, 32)
+    v = O.init_interactions(4, 4, 2, 1, 0.0, "v").reshape(2, 32)
+    c = O.init_interactions(4, 4, 2, 1, 0.0, "c").reshape(2, 32)
+    for k in range(2):
+        assert (h[k, 16:20] == -1).all() and (np.delete(h[k], range(16, 20)) == 1).all()
+        assert (v[k, [0, 4, 8, 12]] == -1).all() and (np.delete(v[k], [0, 4, 8, 12]) == 1).all()
+        neg = [0, 4, 8, 12, 16, 17, 18, 19]
+        assert (c[k, neg] == -1).all() and (np.delete(c[k], neg) == 1).all()
+
+
+def test_flip_ratio():
+    """test_init_interactions.cu:19-43: 10x10, 1000 samples, p=0.15 within 1%."""
+    J = O.init_interactions(10, 10, 1000, 1, 0.15)
+    assert abs((J == -1).mean() - 0.15) / 0.15 < 0.01
+
+
+# -------------------------------------------------- exact spectra (integration)
+
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_transfer_matrix_equals_enumeration(boundary):
+    for seed in (1, 2, 3):
+        for X, Y in ((4, 4), (3, 5), (2, 6)):
+            J = O.init_interactions(X, Y, 1, seed, 0.3)
+            assert np.array_equal(O.exact_counts(J, X, Y, boundary), O.exact_counts(J, X, Y, boundary, brute=True))
+
+
+def test_p0_reachable_energies_4x4():
+    """test_wang_landau_pre_run.cu:601-815: every multiple of 4 except +-28 (periodic); open rule."""
+    J = np.ones(32, np.int8)
+    per = set((np.nonzero(O.exact_counts(J, 4, 4, 0))[0] - 32).tolist())
+    assert per == {e for e in range(-32, 33, 4) if e not in (-28, 28)}
+    opn = set((np.nonzero(O.exact_counts(J, 4, 4, 1))[0] - 32).tolist())
+    want = {e for e in range(-32, 33) if e % 2 == 0 and -24 <= e <= 24 and e not in (22, -22)}
+    assert opn == want
+
+
+@pytest.mark.parametrize("boundary,p", [(0, 0.0), (1, 0.0), (0, 1.0), (1, 0.3)])
+def test_prerun_finds_exact_spectrum_4x4(boundary, p):
+    """integration_prerun_matching_hist_energies.py: the pre-run's reachable set of a
+    4x4 lattice equals the exact enumeration (128 walkers, 10^4 iterations, 20 bins)."""
+    pre = prerun_outputs(4, 4, boundary, p, "i", 12345, 3, 128, 20, 10000)
+    for k in range(3):
+        seen = pre["seen"][k * 65:(k + 1) * 65]
+        J = pre["J"][k * 32:(k + 1) * 32]
+        exact = O.exact_counts(J, 4, 4, boundary) > 0
+        assert np.array_equal(seen.astype(bool), exact)
+
+
+def test_prerun_stored_lattices_match_their_energies():
+    """integration_prerun_check_energies.py: stored lattices' energies recomputed."""
+    pre = prerun_outputs(5, 5, 0, 0.2, "v", 9, 2, 64, 36, 3000)
+    N = 25
+    for k in range(2):
+        for q in range(36):
+            if pre["found_flag"][k * 36 + q]:
+                lat = pre["found_lat"][(k * 36 + q) * N:(k * 36 + q + 1) * N]
+                e = O.calc_energy(0, lat, pre["J"][k * 50:(k + 1) * 50], np.zeros(1, np.int32), 5, 5, 1, 1)[0]
+                assert e == pre["found_energy"][k * 36 + q]
+                s, en, _, ln = O.interval_results(-50, 50, 36, 1, 1.0)
+                assert min((e + 50) // ln, 35) == q
+
+
+# ------------------------------------------------------- test_check_histogram.cu
+
+def _golden_windows():
+    start = np.array([-2, -1, 0, -4, -2, 0, -2, -1, 0], np.int32)
+    end = np.array([-1, 0, 2, -2, 0, 2, -2, -1, 1], np.int32)
+    off_hist = np.array([0, 2, 4, 6, 8, 10, 12, 14] + [16 + 3 * q for q in range(16)] + [64 + q for q in range(8)]
+                        + [72, 74, 76, 78], np.int32)
+    return start, end, off_hist
+
+
+def test_check_histogram_reference_vector():
+    start, end, off_hist = _golden_windows()
+    H = np.full(80, 10, np.uint64)
+    H[0] = 1
+    st = dict(R=3, I=3, W=4, H=H, factor=np.full(36, np.e), cond=np.array([0] * 8 + [1], np.int8),
+              off_hist=off_hist, start=start, end=end, spectrum=np.ones(20, np.int8),
+              off_spec=np.array([0, 7, 16], np.int32), cond_inter=np.ones(3, np.int32))
+    o_check_histogram(st, 0.8)
+    want = np.zeros(80, np.uint64)
+    want[:8] = 10
+    want[72:] = 10
+    want[0] = 1
+    assert np.array_equal(st["H"], want)
+    assert st["cond"].tolist() == [0, 1, 1, 1, 1, 1, 1, 1, 1]
+    wf = np.full(36, np.sqrt(np.e))
+    wf[:4] = np.e
+    wf[32:] = np.e
+    assert np.allclose(st["factor"], wf, rtol=1e-15, atol=0)
+
+
+# ---------------------------------------- test_calc_average_log_g.cu + redistribute
+
+@pytest.mark.parametrize("cond,cond_inter", [([1] * 9, [1, 1, 1]), ([0, 0, 0, 0, 0, 1, 0, 1, 1], [1, 1, 1]),
+                                             ([1] * 9, [-1, -1, 1])])
+def test_average_log_g_reference_vectors(cond, cond_inter):
+    """test_calc_average_log_g.cu:39-408 followed by test_redistribute_g_values.cu."""
+    start, end, off_hist = _golden_windows()
+    logG = np.arange(80, dtype=np.float64)
+    st = dict(R=3, I=3, W=4, logG=logG.copy(), start=start, end=end, spectrum=np.ones(20, np.int8),
+              off_spec=np.array([0, 7, 16], np.int32), cond=np.array(cond, np.int8), off_hist=off_hist,
+              cond_inter=np.array(cond_inter, np.int32))
+    o_average(st)
+    want = logG.copy()
+    for b in range(9):
+        k = b // 3
+        if cond[b] != 1 or cond_inter[k] == -1:
+            continue
+        ln = end[b] - start[b] + 1
+        for i in range(ln):
+            avg = 0.0
+            for w in range(4):
+                avg += logG[off_hist[b * 4 + w] + i] / 4
+            for w in range(4):
+                want[off_hist[b * 4 + w] + i] = avg
+    assert np.array_equal(st["logG"], want)
+    # the test's own expectation (sum of logG/4 per window bin) within 1e-15 relative
+    for b in range(9):
+        if cond[b] != 1 or cond_inter[b // 3] == -1:
+            continue
+        for i in range(end[b] - start[b] + 1):
+            ref = sum(logG[off_hist[b * 4 + w] + i] / 4 for w in range(4))
+            assert abs(st["logG"][off_hist[b * 4] + i] - ref) <= 1e-15 * max(1.0, abs(ref))
+
+
+# -------------------------------------------------------- test_replica_exchange.cu
+
+def test_replica_exchange_flat_log_g():
+    R, I, W = 3, 10, 5
+    T = R * I * W
+    start = np.zeros(R * I, np.int32)
+    end = np.zeros(R * I, np.int32)
+    E = np.zeros(T, np.int32)
+    off_hist = np.zeros(T, np.int32)
+    off_lat = np.zeros(T, np.int32)
+    acc = 0
+    for b in range(R * I):
+        bl, k = b % I, b // I
+        start[b], end[b] = bl + k, bl + k + 4
+        for w in range(W):
+            t = b * W + w
+            E[t], off_hist[t], off_lat[t] = bl + k + 2, acc, t * 9
+            acc += 5
+    st = dict(R=R, I=I, W=W, start=start, end=end, E=E.copy(), off_hist=off_hist, off_lat=off_lat.copy(),
+              logG=np.ones(acc), perm=(np.arange(T) % W).astype(np.int32), off_iter=np.zeros(T, np.uint64),
+              cond_inter=np.ones(R, np.int32))
+    o_exchange(st, 1, 42, global_parity=1)
+    for b in range(R * I):
+        if b % I == I - 1 or b % 2:
+            continue
+        perm = st["perm"][b * W:(b + 1) * W]
+        assert sorted(perm.tolist()) == list(range(W))
+        for w in range(W):
+            t, o = b * W + w, (b + 1) * W + perm[w]
+            assert st["off_lat"][t] == off_lat[o] and st["off_lat"][o] == off_lat[t]
+            assert st["E"][t] == E[o] and st["E"][o] == E[t]
+        # walker 0 consumed W-1 shuffle draws + 1 acceptance draw, the others 1
+        assert st["off_iter"][b * W] == W and (st["off_iter"][b * W + 1:(b + 1) * W] == 1).all()
+
+
+# --------------------------------------------------------------- main-run loop
+
+def test_oracle_mainrun_normalisation_and_spectrum():
+    """integration_mainrun.py: energies of the result == pre-run spectrum,
+    logsumexp(log g) == N ln 2 (5x5, p = 0.2)."""
+    X = Y = 5
+    N = X * Y
+    pre = prerun_outputs(X, Y, 0, 0.2, "i", 1234, 1, 128, 36, 10000)
+    I, W = 10, 4
+    start = np.zeros(I, np.int32)
+    end = np.zeros(I, np.int32)
+    off_hist = np.zeros(I * W, np.int32)
+    n_log = C.c_longlong(0)
+    ci = np.zeros(1, np.int32)
+    outer = C.c_longlong(0)
+    flips = C.c_longlong(0)
+    args = (X, Y, 0, 1, I, W, C.c_float(0.25), 0.8, 0.01, 1000, 20, 1, 0, 1234, 0, O.ptr(pre["seen"]),
+            O.ptr(pre["J"]), O.ptr(pre["found_lat"]), O.ptr(pre["found_flag"]), O.ptr(pre["found_energy"]), 36,
+            O.ptr(start), O.ptr(end), O.ptr(off_hist))
+    O.lib().orc_mainrun(*args, None, C.byref(n_log), O.ptr(ci), C.byref(outer), C.byref(flips))
+    logG = np.zeros(n_log.value)
+    st = O.lib().orc_mainrun(*args, O.ptr(logG), C.byref(n_log), O.ptr(ci), C.byref(outer), C.byref(flips))
+    assert st == 0 and ci[0] == -1
+    Eo = np.zeros(4 * N + 1, np.int32)
+    Go = np.zeros(4 * N + 1)
+    nout = C.c_int(0)
+    assert O.lib().orc_stitch(O.ptr(logG), O.ptr(start), O.ptr(end), I, W, X, Y, O.ptr(Eo), O.ptr(Go), len(Eo),
+                              C.byref(nout)) == 0
+    E, G = Eo[:nout.value], Go[:nout.value]
+    assert abs(np.logaddexp.reduce(G) - N * np.log(2)) < 1e-12
+    spectrum = set((np.nonzero(pre["seen"])[0] - 2 * N).tolist())
+    assert set(E.tolist()) == spectrum
+
+
+def test_mainrun_state_windows_cover_spectrum():
+    pre = prerun_outputs(6, 6, 0, 0.04, "i", 12345, 2, 128, 32, 1000)
+    st = mainrun_state(pre, 10, 3, 0.25)
+    for k in range(2):
+        s = st["start"][k * 10:(k + 1) * 10]
+        e = st["end"][k * 10:(k + 1) * 10]
+        assert (s[1:] <= e[:-1]).all()  # overlapping cover
+        assert e[-1] - s[0] + 1 == (st["off_spec"][1] if k == 0 else len(st["spectrum"]) - st["off_spec"][1])
