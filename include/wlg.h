@@ -222,6 +222,16 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
 wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* win_start,
                          int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset);
 
+/* Plain form: the same problems computed with the reference's own structure
+ * (prerun.cu:36-154, mainrun.cu:115-421) on the operators above — one
+ * launch per operation, one thread per walker, state in global memory,
+ * outer loop on the host with a device->host check per iteration.
+ * Problems sharing all parameters but `sample` run as one R-sample run and
+ * must hold samples 0..R-1.  Same outputs as wlg_solve; caller-allocated
+ * nothing on the device (buffers are allocated and freed per call). */
+wlg_status wlg_solve_plain(const wlg_problem* problems, int n, wlg_result* results, int* energies, double* log_g,
+                           long long capacity, wlg_stream stream, long long* kernel_launches);
+
 /* What the last wlg_solve / wlg_solve_raw did: time by phase in
  * milliseconds (device phases by CUDA events on the context's stream, host
  * phases by the host clock), bytes copied host->device and device->host,

@@ -47,6 +47,7 @@ SIGNATURES = {
     "wlg_solve": [P, P, i32, P, P, P, i64],
     "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
     "wlg_last_stats": [P, P],
+    "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
     "wlg_class_log_probs": [P, P, P, P, i32, f64, P, P],
 }
 _RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p}
@@ -193,6 +194,22 @@ class Context:
 class Stats(C.Structure):
     _fields_ = [("pre_ms", f64), ("handoff_ms", f64), ("main_ms", f64), ("stitch_ms", f64), ("h2d_bytes", i64),
                 ("d2h_bytes", i64), ("kernel_launches", i32)]
+
+
+def solve_plain(problems, stream=None):
+    """The plain (reference-structured) form: list of (Result, energies, log_g), kernel launch count."""
+    import numpy as np
+    n = len(problems)
+    arr = (Problem * n)(*problems)
+    res = (Result * n)()
+    cap = sum(4 * p.X * p.Y + 1 for p in problems)
+    E = np.zeros(max(cap, 1), np.int32)
+    G = np.zeros(max(cap, 1), np.float64)
+    launches = C.c_longlong(0)
+    call("wlg_solve_plain", C.cast(arr, P), n, C.cast(res, P), E.ctypes.data_as(P), G.ctypes.data_as(P), cap,
+         stream, C.byref(launches))
+    return [(r, E[r.offset:r.offset + r.n_energies].copy(), G[r.offset:r.offset + r.n_energies].copy())
+            for r in res], launches.value
 
 
 def class_log_probs(curves, prob):

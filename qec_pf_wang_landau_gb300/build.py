@@ -1,8 +1,8 @@
 """Build recipe for the engine's shared library (``libwlg.so``).
 
-Every ``csrc/*.cu`` and ``csrc/*.cpp`` translation unit is compiled in
-parallel for sm_103a only and linked into one in-tree shared library exposing
-the C ABI of ``include/wlg.h``.  Host code is built with
+Every ``csrc/*.cu`` translation unit is compiled by nvcc for sm_103a only,
+every ``csrc/*.cpp`` host unit by g++, in parallel, and all are linked into
+one in-tree shared library exposing the C ABI of ``include/wlg.h``.  Host code is built with
 ``-ffp-contract=off`` so float expressions round identically on x86 and Arm.
 """
 
@@ -11,6 +11,7 @@ from __future__ import annotations
 import concurrent.futures as cf
 import glob
 import os
+import shutil
 import subprocess
 
 PKG = os.path.dirname(os.path.abspath(__file__))
@@ -22,6 +23,7 @@ LIB = os.path.join(PKG, "libwlg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++20", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include")]
+CXX_FLAGS = ["-std=c++20", "-O3", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(ROOT, "include")]
 
 
 def _sources():
@@ -33,15 +35,20 @@ def _headers():
                   + glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
+def _cuda_home() -> str:
+    nvcc = shutil.which("nvcc")
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc))) if nvcc else "/usr/local/cuda"
+
+
 def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj
-    cmd = ["nvcc", *NVCC_FLAGS, "-c", src, "-o", obj + ".tmp"]
     if src.endswith(".cpp"):
-        cmd.insert(1, "-x")
-        cmd.insert(2, "cu")
+        cmd = ["g++", *CXX_FLAGS, "-I" + os.path.join(_cuda_home(), "include"), "-c", src, "-o", obj + ".tmp"]
+    else:
+        cmd = ["nvcc", *NVCC_FLAGS, "-c", src, "-o", obj + ".tmp"]
     subprocess.run(cmd, check=True)
     os.replace(obj + ".tmp", obj)
     return obj

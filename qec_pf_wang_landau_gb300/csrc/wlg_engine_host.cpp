@@ -20,7 +20,7 @@
 #include "../../include/wlg.h"
 #include "wlg_engine.h"
 #include "wlg_internal.h"
-#include "wlg_rng.cuh"
+#include "wlg_keys.h"
 
 namespace wlg {
 
@@ -528,6 +528,8 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     ctx->t_main = 0;
     return WLG_OK;
   }
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   std::map<std::pair<int, int>, std::vector<int>> groups;
   for (int i = 0; i < m; ++i) groups[{prep.main[i].N <= 64 ? 1 : 0, prep.main[i].team}].push_back(i);
   std::vector<int> order;
@@ -545,6 +547,9 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     int per_cta = team <= 256 ? 256 / team : 1;
     per_cta = std::min(per_cta, (227 * 1024) / bytes);
     if (team > 32) per_cta = std::min(per_cta, 15);
+    // small batches: spread the teams over all SMs (>= 2 CTAs per SM) rather
+    // than packing them into few CTAs
+    per_cta = std::min(per_cta, static_cast<int>(idx.size()) / (2 * sms));
     per_cta = std::max(per_cta, 1);
     launches.emplace_back(reg, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()));
     order.insert(order.end(), idx.begin(), idx.end());

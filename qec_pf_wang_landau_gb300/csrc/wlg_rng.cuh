@@ -17,6 +17,8 @@
 
 #include <cstdint>
 
+#include "wlg_keys.h"
+
 namespace wlg {
 
 constexpr uint32_t kPhiloxMulA = 0xD2511F53u;
@@ -83,21 +85,5 @@ struct Stream {
 
   __device__ __forceinline__ float uniform() { return unit_float(raw()); }
 };
-
-// The reference forms Philox keys from `seed + sample` with three integer
-// promotions; they agree for non-negative seeds that do not overflow.
-__host__ __device__ __forceinline__ uint64_t key_u32(int seed, uint64_t k)  // wl.cu:448, :505, :1074
-{
-  return static_cast<uint32_t>(static_cast<uint32_t>(seed) + static_cast<uint32_t>(k));
-}
-__host__ __device__ __forceinline__ uint64_t key_i32(int seed, uint64_t k)  // wl.cu:796, :875
-{
-  return static_cast<uint64_t>(
-    static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(seed) + static_cast<uint32_t>(k))));
-}
-__host__ __device__ __forceinline__ uint64_t key_size(int seed, uint64_t k)  // wl.cu:380
-{
-  return static_cast<uint64_t>(static_cast<int64_t>(seed)) + k;
-}
 
 }  // namespace wlg

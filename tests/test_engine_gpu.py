@@ -153,3 +153,20 @@ def test_class_log_probs_normalised(cuda):
     exact = np.array(exact) - np.logaddexp.reduce(exact)
     assert np.argmax(lp) == np.argmax(exact)
     assert np.abs(np.exp(lp) - np.exp(exact)).max() < 0.05
+
+
+@pytest.mark.parametrize("cls,xc,xmode,gpar,I", [("i", 20, 1, 0, 10), ("c", 1, 0, 1, 7), ("h", 3, 1, 1, 5)])
+def test_plain_form_equals_batched_form(cuda, cls, xc, xmode, gpar, I):
+    """The reference-structured plain form and the persistent batched form
+    compute identical results (same streams, same FP64 operation order)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = [wlg.problem(6, 6, prob=0.04, error_class=cls, seed=2024, sample=k, pre_walkers=128, pre_intervals=32,
+                         pre_iterations=1000, intervals=I, walkers_per_interval=3, beta=0.01, iterations=500,
+                         exchange_every=xc, exchange_mode=xmode, global_parity=gpar) for k in range(6)]
+    plain, launches = wlg.solve_plain(probs)
+    batched = wlg.Context(0).solve(probs)
+    assert launches > 10
+    for (r1, E1, G1), (r2, E2, G2) in zip(plain, batched):
+        assert r1.status == r2.status == 0
+        assert r1.outer_iterations == r2.outer_iterations and r1.flips == r2.flips
+        assert np.array_equal(E1, E2) and np.array_equal(G1, G2)
