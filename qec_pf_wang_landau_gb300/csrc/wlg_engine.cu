@@ -166,7 +166,8 @@ struct Team {
 };
 
 // Site of a draw: trunc(double(u) * ((N-1) + 0.999999)) (wl.cu:63-65),
-// computed in FP32 unless the product lies within site_eps of an integer.
+// computed in FP32 unless the product lies within site_eps (= N*2^-21, four
+// times the FP32 error bound) of an integer.
 __device__ __forceinline__ int pick_site(uint32_t x, const MainDesc& d)
 {
   const float uf = unit_float(x);
@@ -175,17 +176,6 @@ __device__ __forceinline__ int pick_site(uint32_t x, const MainDesc& d)
   const float fr = pr - static_cast<float>(s);
   if (fr < d.site_eps || fr > 1.0f - d.site_eps) s = static_cast<int>(trunc(static_cast<double>(uf) * d.site_scale));
   return s;
-}
-
-// u < min(1, exp(delta)) with delta = logg_old - logg_new (wl.cu:1113-1116).
-__device__ __forceinline__ bool accept_move(uint32_t x, double delta)
-{
-  const float u = unit_float(x);
-  if (delta >= 0.0) return u < 1.0f;
-  const float ef = expf(static_cast<float>(delta));
-  if (u < ef * (1.0f - kBand)) return true;
-  if (u > ef * (1.0f + kBand)) return false;
-  return static_cast<double>(u) < fmin(1.0, exp(delta));
 }
 
 struct Lat {
@@ -205,12 +195,12 @@ __device__ __forceinline__ uint32_t spin_bit(const Lat& l, int q)
 }
 
 template <bool kReg>
-__device__ __forceinline__ void flip_spin(Lat& l, int q)
+__device__ __forceinline__ void flip_spin(Lat& l, int q, bool doit)
 {
   if constexpr (kReg) {
-    l.r ^= 1ull << q;
+    l.r ^= static_cast<uint64_t>(doit) << q;
   } else {
-    l.s[(q >> 5) * l.P] ^= 1u << (q & 31);
+    if (doit) l.s[(q >> 5) * l.P] ^= 1u << (q & 31);
   }
 }
 
@@ -224,28 +214,39 @@ __device__ __forceinline__ uint32_t bond_bit(uint64_t reg, const uint32_t* sm, i
   }
 }
 
+struct Nbr {
+  int up, dn, lf, rt, i, j;
+};
+
+__device__ __forceinline__ Nbr neighbours(int site, const MainDesc& d)
+{
+  Nbr n;
+  n.i = static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20);
+  n.j = site - n.i * d.Y;
+  n.up = (n.i == 0 ? d.X - 1 : n.i - 1) * d.Y + n.j;
+  n.dn = (n.i == d.X - 1 ? 0 : n.i + 1) * d.Y + n.j;
+  n.lf = n.i * d.Y + (n.j == 0 ? d.Y - 1 : n.j - 1);
+  n.rt = n.i * d.Y + (n.j == d.Y - 1 ? 0 : n.j + 1);
+  return n;
+}
+
 // Energy after flipping `site` (wl.cu:52-156 on bits: a neighbour term
 // s_nb * J is -1 exactly when its spin bit and bond bit differ).
 template <bool kReg>
 __device__ __forceinline__ int energy_after_flip(const Lat& l, uint64_t JR, uint64_t JD, const uint32_t* Jr_s,
                                                  const uint32_t* Jd_s, int site, int E, const MainDesc& d)
 {
-  const int i = static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20);
-  const int j = site - i * d.Y;
-  const int up = (i == 0 ? d.X - 1 : i - 1) * d.Y + j;
-  const int dn = (i == d.X - 1 ? 0 : i + 1) * d.Y + j;
-  const int lf = i * d.Y + (j == 0 ? d.Y - 1 : j - 1);
-  const int rt = i * d.Y + (j == d.Y - 1 ? 0 : j + 1);
-  const int t_up = static_cast<int>(spin_bit<kReg>(l, up) ^ bond_bit<kReg>(JD, Jd_s, up));
-  const int t_lf = static_cast<int>(spin_bit<kReg>(l, lf) ^ bond_bit<kReg>(JR, Jr_s, lf));
-  const int t_dn = static_cast<int>(spin_bit<kReg>(l, dn) ^ bond_bit<kReg>(JD, Jd_s, site));
-  const int t_rt = static_cast<int>(spin_bit<kReg>(l, rt) ^ bond_bit<kReg>(JR, Jr_s, site));
+  const Nbr n = neighbours(site, d);
+  const int t_up = static_cast<int>(spin_bit<kReg>(l, n.up) ^ bond_bit<kReg>(JD, Jd_s, n.up));
+  const int t_lf = static_cast<int>(spin_bit<kReg>(l, n.lf) ^ bond_bit<kReg>(JR, Jr_s, n.lf));
+  const int t_dn = static_cast<int>(spin_bit<kReg>(l, n.dn) ^ bond_bit<kReg>(JD, Jd_s, site));
+  const int t_rt = static_cast<int>(spin_bit<kReg>(l, n.rt) ^ bond_bit<kReg>(JR, Jr_s, site));
   int sigma;
   if (d.boundary == 0) {
     sigma = 4 - 2 * (t_up + t_lf + t_dn + t_rt);
   } else {
-    sigma = (i > 0 ? 1 - 2 * t_up : 0) + (j > 0 ? 1 - 2 * t_lf : 0) + (i < d.X - 1 ? 1 - 2 * t_dn : 0) +
-            (j < d.Y - 1 ? 1 - 2 * t_rt : 0);
+    sigma = (n.i > 0 ? 1 - 2 * t_up : 0) + (n.j > 0 ? 1 - 2 * t_lf : 0) + (n.i < d.X - 1 ? 1 - 2 * t_dn : 0) +
+            (n.j < d.Y - 1 ? 1 - 2 * t_rt : 0);
   }
   const int s = 1 - 2 * static_cast<int>(spin_bit<kReg>(l, site));
   return E + 2 * s * sigma;
@@ -253,7 +254,17 @@ __device__ __forceinline__ int energy_after_flip(const Lat& l, uint64_t JR, uint
 
 __device__ __forceinline__ bool mask_has(const uint32_t* mask, int c) { return (mask[c >> 5] >> (c & 31)) & 1u; }
 
-template <bool kReg>
+__device__ __forceinline__ uint32_t pick_word(const uint4& A, const uint4& B, int i)  // i in [0, 4]
+{
+  uint32_t v = A.x;
+  v = (i == 1) ? A.y : v;
+  v = (i == 2) ? A.z : v;
+  v = (i == 3) ? A.w : v;
+  v = (i == 4) ? B.x : v;
+  return v;
+}
+
+template <bool kReg, bool kTable>
 __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base,
                             const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
                             const int* __restrict__ winpool, const uint32_t* __restrict__ maskpool,
@@ -261,14 +272,16 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
                             uint32_t* __restrict__ dumppool)
 {
   const int P = team.size;
-  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg);
+  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg, kTable ? d.N : 0);
   double* G = reinterpret_cast<double*>(base + lay.off_G);
+  float* Gf = reinterpret_cast<float*>(base + lay.off_Gf);
   uint32_t* H = reinterpret_cast<uint32_t*>(base + lay.off_H);
   uint32_t* lat_s = reinterpret_cast<uint32_t*>(base + lay.off_lat);
   int* E_s = reinterpret_cast<int*>(base + lay.off_E);
   int* perm = reinterpret_cast<int*>(base + lay.off_perm);
   uint32_t* mask = reinterpret_cast<uint32_t*>(base + lay.off_mask);
   uint32_t* Js = reinterpret_cast<uint32_t*>(base + lay.off_J);
+  ulonglong2* nbt = reinterpret_cast<ulonglong2*>(base + lay.off_nbt);
   double* fwin = reinterpret_cast<double*>(base + lay.off_f);
   int* cond = reinterpret_cast<int*>(base + lay.off_cond);
   int* flat = reinterpret_cast<int*>(base + lay.off_flat);
@@ -291,6 +304,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   }
   for (int c = 0; c < d.L; ++c) {
     G[c * P + t] = 0.0;
+    Gf[c * P + t] = 0.0f;
     H[c * P + t] = 0u;
   }
   if (t < 8) misc[t] = 0;
@@ -307,6 +321,33 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   }
   const uint32_t* Jr_s = Js;
   const uint32_t* Jd_s = Js + d.nwL;
+  if constexpr (kTable) {
+    // neighbour table: bits of the neighbours of each site, and of those
+    // whose connecting bond is -1 (X, Y >= 3, so the 4 neighbours differ)
+    for (int site = t; site < d.N; site += P) {
+      const Nbr n = neighbours(site, d);
+      uint64_t m = 0, bnd = 0;
+      const bool has_up = d.boundary == 0 || n.i > 0, has_dn = d.boundary == 0 || n.i < d.X - 1;
+      const bool has_lf = d.boundary == 0 || n.j > 0, has_rt = d.boundary == 0 || n.j < d.Y - 1;
+      if (has_up) {
+        m |= 1ull << n.up;
+        bnd |= static_cast<uint64_t>((JD >> n.up) & 1ull) << n.up;
+      }
+      if (has_lf) {
+        m |= 1ull << n.lf;
+        bnd |= static_cast<uint64_t>((JR >> n.lf) & 1ull) << n.lf;
+      }
+      if (has_dn) {
+        m |= 1ull << n.dn;
+        bnd |= static_cast<uint64_t>((JD >> site) & 1ull) << n.dn;
+      }
+      if (has_rt) {
+        m |= 1ull << n.rt;
+        bnd |= static_cast<uint64_t>((JR >> site) & 1ull) << n.rt;
+      }
+      nbt[site] = make_ulonglong2(m, bnd);
+    }
+  }
   Lat lt;
   lt.P = P;
   lt.s = lat_s + t;
@@ -326,6 +367,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   const double reset_lim = exp(d.beta);  // wl.cu:609
   const int lo = live ? w_start[b] : 0, hi = live ? w_end[b] : 0, bb = live ? w_base[b] : 0;
   const int step_mask = (1 << d.lg) - 1;
+  const int span = d.e_max - d.e_min;
+  const int Lm1 = d.L - 1;
 
   long long outer = 0;
   long long counter = 1;
@@ -337,59 +380,107 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       status = WLG_ERR_TIMEOUT;
       break;
     }
-    // ---- WL sweep (wl.cu:1077-1175)
+    // ---- WL sweep (wl.cu:1077-1175).  One uniform, branch-free step body:
+    // the acceptance draw is peeked and used only for in-window proposals,
+    // the Philox block after next is computed speculatively every step.
     if (live) {
       const bool frozen = cond[b] != 0;
       const double lnf = log(fwin[b]);
+      const float lnf_f = static_cast<float>(lnf);
       int c_cur = (E - bb) >> d.lg;
       double g_cur = G[c_cur * P + t];
+      float gfb = Gf[c_cur * P + t];  // float of g_cur at the last change of bin
       uint32_t h_cur = H[c_cur * P + t];
+      int k = 0;                      // ln f increments since then
+      uint64_t pos = rng.pos;
+      uint64_t blk = pos >> 2;
+      uint4 A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), rng.s0, rng.s1, rng.k0, rng.k1);
+      uint4 B = philox10(static_cast<uint32_t>(blk + 1), static_cast<uint32_t>((blk + 1) >> 32), rng.s0, rng.s1,
+                         rng.k0, rng.k1);
       for (int it = 0; it < d.n_iter; ++it) {
-        const int site = pick_site(rng.raw(), d);
-        const int En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
+        const uint64_t nx = blk + 2;
+        const uint4 Cn = philox10(static_cast<uint32_t>(nx), static_cast<uint32_t>(nx >> 32), rng.s0, rng.s1, rng.k0,
+                                  rng.k1);
+        const int q = static_cast<int>(pos - (blk << 2));
+        const uint32_t x1 = pick_word(A, B, q);
+        const uint32_t x2 = pick_word(A, B, q + 1);
+        const int site = pick_site(x1, d);
+        int En;
+        if constexpr (kTable) {
+          const ulonglong2 nt = nbt[site];
+          const int unsat = __popcll((lt.r ^ nt.y) & nt.x);
+          const int deg = __popcll(nt.x);
+          const int sb = static_cast<int>((lt.r >> site) & 1ull);
+          En = E + 2 * (1 - 2 * sb) * (deg - 2 * unsat);
+        } else {
+          En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
+        }
         const int rel = En - d.e_min;
-        if (rel < 0 || En > d.e_max || (rel & step_mask) != 0 || !mask_has(mask, rel >> d.lg)) {
-          misc[1] = 1;  // found a new energy (wl.cu:1091-1104): the problem stops
+        const int relc = min(max(rel, 0), span);
+        const bool bad = rel != relc || (rel & step_mask) != 0 || !mask_has(mask, relc >> d.lg);
+        const bool inside = En >= lo && En <= hi;
+        const int c_new = min(max((En - bb) >> d.lg, 0), Lm1);
+        const bool same = c_new == c_cur;
+        const float gfn = Gf[c_new * P + t];
+        // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) from FP32 values
+        // with a proven error bound eps on the exponent; the reference's FP64
+        // expression decides whenever the bound does not.
+        const float u2 = unit_float(x2);
+        const float kl = static_cast<float>(k) * lnf_f;
+        const float df = (gfb - gfn) + kl;
+        const float eps = 0x1p-22f * (gfb + gfn + kl + fabsf(df));
+        const bool nonneg = same || df - eps >= 0.0f;
+        const float e = __expf(df);
+        const float r = 1.1f * (eps + (2.0f + 1.2f * fabsf(df)) * 0x1p-23f) + 0x1p-22f;
+        const float t_lo = e * (1.0f - r), t_hi = e * (1.0f + r);
+        bool acc = nonneg ? (u2 < 1.0f) : (u2 < t_lo);
+        const bool known = nonneg || (df + eps < 0.0f && (u2 < t_lo || u2 >= t_hi));
+        if (inside && !known) {
+          const double gn = G[c_new * P + t];
+          acc = static_cast<double>(u2) < fmin(1.0, exp(g_cur - gn));
+        }
+        if (bad) {  // wl.cu:1091-1104: a new energy stops the problem
+          ++pos;
+          misc[1] = 1;
           misc[2] = En;
           break;
         }
-        if (En < lo || En > hi) {
-          if (!frozen) {
-            g_cur += lnf;
-            h_cur += 1u;
-          }
-          continue;
-        }
-        const int c_new = (En - bb) >> d.lg;
-        const double g_new = (c_new == c_cur) ? g_cur : G[c_new * P + t];
-        const bool acc = accept_move(rng.raw(), g_cur - g_new);
-        if (frozen) {
-          if (acc) {
-            flip_spin<kReg>(lt, site);
-            E = En;
-            c_cur = c_new;
-            g_cur = g_new;
-          }
-          continue;
-        }
-        if (acc) {
-          flip_spin<kReg>(lt, site);
-          if (c_new != c_cur) {
+        acc = acc && inside;
+        flip_spin<kReg>(lt, site, acc);
+        E = acc ? En : E;
+        const bool change = acc && !same;
+        if (!frozen) {
+          if (change) {
             G[c_cur * P + t] = g_cur;
+            Gf[c_cur * P + t] = static_cast<float>(g_cur);
             H[c_cur * P + t] = h_cur;
-            g_cur = g_new;
+            g_cur = G[c_new * P + t];
             h_cur = H[c_new * P + t];
+            gfb = gfn;
+            k = 0;
             c_cur = c_new;
           }
-          E = En;
+          g_cur += lnf;
+          h_cur += 1u;
+          ++k;
+        } else if (change) {
+          g_cur = G[c_new * P + t];
+          gfb = gfn;
+          c_cur = c_new;
         }
-        g_cur += lnf;
-        h_cur += 1u;
+        pos += inside ? 2 : 1;
+        const bool adv = (pos >> 2) != blk;
+        A = adv ? B : A;
+        B = adv ? Cn : B;
+        blk = adv ? blk + 1 : blk;
       }
       if (!frozen) {
         G[c_cur * P + t] = g_cur;
+        Gf[c_cur * P + t] = static_cast<float>(g_cur);
         H[c_cur * P + t] = h_cur;
       }
+      rng.pos = pos;
+      rng.refill();
     }
     team.sync();
     ++outer;
@@ -431,7 +522,11 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       if (mask_has(mask, ((w_base[wb] - d.e_min) >> d.lg) + c)) {
         for (int v = 0; v < W; ++v) avg += G[c * P + wb * W + v] / W;
       }
-      for (int v = 0; v < W; ++v) G[c * P + wb * W + v] = avg;
+      const float avg_f = static_cast<float>(avg);
+      for (int v = 0; v < W; ++v) {
+        G[c * P + wb * W + v] = avg;
+        Gf[c * P + wb * W + v] = avg_f;
+      }
     }
     team.sync();
     // ---- reset and convergence (wl.cu:596-613, :662-708, mainrun.cu:243, :342-344)
@@ -544,7 +639,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   team.sync();
 }
 
-template <bool kReg, int kMaxThreads>
+template <bool kReg, bool kTable, int kMaxThreads>
 __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __restrict__ descs, const int* __restrict__ order,
                                                      int n, int team_size, int team_bytes, int* __restrict__ next,
                                                      const uint32_t* __restrict__ Jpool,
@@ -568,7 +663,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __re
     if (q >= n) return;
     const int p = order[q];
     const MainDesc d = descs[p];
-    run_problem<kReg>(d, p, team, t, base, Jpool, latpool, winpool, maskpool, outpool, results, dumppool);
+    run_problem<kReg, kTable>(d, p, team, t, base, Jpool, latpool, winpool, maskpool, outpool, results, dumppool);
   }
 }
 
@@ -588,25 +683,30 @@ wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem
   return launch_status();
 }
 
-template <bool kReg, int kMaxThreads>
-struct MainKernel {
-  static decltype(&k_main_batch<kReg, kMaxThreads>) fn() { return &k_main_batch<kReg, kMaxThreads>; }
-};
-
 using MainFn = void (*)(const MainDesc*, const int*, int, int, int, int*, const uint32_t*, const uint32_t*, const int*,
                         const uint32_t*, double*, MainResult*, uint32_t*);
 
-MainFn main_fn(bool reg, int cta_threads)
+// variant: 0 = spins in shared memory, 1 = spins in a register, 2 = register
+// spins + neighbour table
+MainFn main_fn(int variant, int cta_threads)
 {
-  if (cta_threads <= 256) return reg ? MainKernel<true, 256>::fn() : MainKernel<false, 256>::fn();
-  return reg ? MainKernel<true, 1024>::fn() : MainKernel<false, 1024>::fn();
+  if (cta_threads <= 256) {
+    if (variant == 2) return &k_main_batch<true, true, 256>;
+    return variant == 1 ? &k_main_batch<true, false, 256> : &k_main_batch<false, false, 256>;
+  }
+  if (cta_threads <= 512) {
+    if (variant == 2) return &k_main_batch<true, true, 512>;
+    return variant == 1 ? &k_main_batch<true, false, 512> : &k_main_batch<false, false, 512>;
+  }
+  if (variant == 2) return &k_main_batch<true, true, 1024>;
+  return variant == 1 ? &k_main_batch<true, false, 1024> : &k_main_batch<false, false, 1024>;
 }
 
 // Returns the number of resident CTAs the launch may use (0 if the
 // configuration does not fit).
-int main_batch_capacity(bool reg, int cta_threads, int smem)
+int main_batch_capacity(int variant, int cta_threads, int smem)
 {
-  MainFn fn = main_fn(reg, cta_threads);
+  MainFn fn = main_fn(variant, cta_threads);
   int per_sm = 0;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, cta_threads, smem) != cudaSuccess) return 0;
@@ -616,7 +716,7 @@ int main_batch_capacity(bool reg, int cta_threads, int smem)
   return per_sm * sms;
 }
 
-wlg_status launch_main_batch(bool reg, const MainDesc* d_descs, const int* d_order, int n, int team_size,
+wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
                              int team_bytes, int teams_per_cta, int grid, int* d_next, const uint32_t* Jpool,
                              const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
                              MainResult* results, uint32_t* dumppool, cudaStream_t s)
@@ -624,7 +724,7 @@ wlg_status launch_main_batch(bool reg, const MainDesc* d_descs, const int* d_ord
   if (n == 0) return WLG_OK;
   const int threads = team_size * teams_per_cta;
   const int smem = team_bytes * teams_per_cta;
-  MainFn fn = main_fn(reg, threads);
+  MainFn fn = main_fn(variant, threads);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return WLG_ERR_CUDA;
   fn<<<grid, threads, smem, s>>>(d_descs, d_order, n, team_size, team_bytes, d_next, Jpool, latpool, winpool,
                                  maskpool, outpool, results, dumppool);

@@ -72,18 +72,23 @@ struct MainResult {
 
 // Team shared-memory layout of a problem (bytes, 16-byte aligned pieces).
 struct TeamLayout {
-  int off_G, off_H, off_lat, off_E, off_perm, off_mask, off_J, off_f, off_cond, off_flat, off_win, off_misc;
+  int off_G, off_Gf, off_H, off_lat, off_E, off_perm, off_mask, off_J, off_nbt, off_f, off_cond, off_flat, off_win,
+    off_misc;
   int bytes;
 };
 
 WLG_HD inline int align16(int x) { return (x + 15) & ~15; }
 
-WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, bool reg_lattice)
+// reg_lattice: spins in a register (N <= 64); nbt_sites: sites of the
+// neighbour table (0 when the table is not used).
+WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, bool reg_lattice, int nbt_sites)
 {
   TeamLayout t{};
   int o = 0;
   t.off_G = o;
   o = align16(o + 8 * L * team);
+  t.off_Gf = o;
+  o = align16(o + 4 * L * team);
   t.off_H = o;
   o = align16(o + 4 * L * team);
   t.off_lat = o;
@@ -96,6 +101,8 @@ WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, b
   o = align16(o + 4 * nwM);
   t.off_J = o;
   o = align16(o + 4 * 2 * nwL);
+  t.off_nbt = o;
+  o = align16(o + 16 * nbt_sites);
   t.off_f = o;
   o = align16(o + 8 * I);
   t.off_cond = o;

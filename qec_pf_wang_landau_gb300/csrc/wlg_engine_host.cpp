@@ -26,8 +26,8 @@ namespace wlg {
 
 wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem, int8_t* Jpool, uint8_t* seen_pool,
                             int8_t* found_pool, int* fflag_pool, cudaStream_t s);
-int main_batch_capacity(bool reg, int cta_threads, int smem);
-wlg_status launch_main_batch(bool reg, const MainDesc* d_descs, const int* d_order, int n, int team_size,
+int main_batch_capacity(int variant, int cta_threads, int smem);
+wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
                              int team_bytes, int teams_per_cta, int grid, int* d_next, const uint32_t* Jpool,
                              const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
                              MainResult* results, uint32_t* dumppool, cudaStream_t s);
@@ -530,17 +530,21 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
   }
   int sms = 1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  // variant: 0 spins in shared memory, 1 spins in a register, 2 register
+  // spins + neighbour table (4 distinct neighbours: X, Y >= 3)
+  auto variant_of = [](const MainDesc& d) { return d.N > 64 ? 0 : (d.X >= 3 && d.Y >= 3 ? 2 : 1); };
   std::map<std::pair<int, int>, std::vector<int>> groups;
-  for (int i = 0; i < m; ++i) groups[{prep.main[i].N <= 64 ? 1 : 0, prep.main[i].team}].push_back(i);
+  for (int i = 0; i < m; ++i) groups[{variant_of(prep.main[i]), prep.main[i].team}].push_back(i);
   std::vector<int> order;
-  std::vector<std::tuple<bool, int, int, int, int, int>> launches;  // reg, team, bytes, per_cta, first, count
+  std::vector<std::tuple<int, int, int, int, int, int>> launches;  // variant, team, bytes, per_cta, first, count
   for (const auto& [key, idx] : groups) {
-    const bool reg = key.first == 1;
+    const int variant = key.first;
     const int team = key.second;
     int bytes = 0;
     for (int i : idx) {
       const MainDesc& d = prep.main[i];
-      bytes = std::max(bytes, wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, reg).bytes + 16);
+      bytes = std::max(bytes,
+                       wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, variant != 0, variant == 2 ? d.N : 0).bytes + 16);
     }
     bytes = wlg::align16(bytes);
     if (bytes > 227 * 1024) return fail(ctx, WLG_ERR_INVALID, "problem state exceeds shared memory");
@@ -551,7 +555,7 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     // than packing them into few CTAs
     per_cta = std::min(per_cta, static_cast<int>(idx.size()) / (2 * sms));
     per_cta = std::max(per_cta, 1);
-    launches.emplace_back(reg, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()));
+    launches.emplace_back(variant, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()));
     order.insert(order.end(), idx.begin(), idx.end());
   }
   if ((st = upload(ctx, ctx->main_desc, prep.main)) != WLG_OK) return st;
@@ -566,11 +570,11 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
   cudaMemsetAsync(ctx->next.p, 0, launches.size() * sizeof(int), ctx->stream);
   cudaEventRecord(ctx->ev[2], ctx->stream);
   for (size_t g = 0; g < launches.size(); ++g) {
-    const auto [reg, team, bytes, per_cta, first, count] = launches[g];
-    const int cap = wlg::main_batch_capacity(reg, team * per_cta, bytes * per_cta);
+    const auto [variant, team, bytes, per_cta, first, count] = launches[g];
+    const int cap = wlg::main_batch_capacity(variant, team * per_cta, bytes * per_cta);
     if (cap <= 0) return fail(ctx, WLG_ERR_CUDA, "main-run configuration does not fit an SM");
     const int grid = std::min(cap, (count + per_cta - 1) / per_cta);
-    st = wlg::launch_main_batch(reg, static_cast<const MainDesc*>(ctx->main_desc.p),
+    st = wlg::launch_main_batch(variant, static_cast<const MainDesc*>(ctx->main_desc.p),
                                 static_cast<const int*>(ctx->order.p) + first, count, team, bytes, per_cta, grid,
                                 static_cast<int*>(ctx->next.p) + g, static_cast<const uint32_t*>(ctx->Jw.p),
                                 static_cast<const uint32_t*>(ctx->latw.p), static_cast<const int*>(ctx->win.p),
