@@ -166,3 +166,56 @@ def run_problems(problems, threads):
     fl = np.zeros(n, np.int64)
     lib().orc_run_problems(C.cast(arr, C.c_void_p), n, threads, ptr(st), ptr(outer), ptr(fl))
     return st, outer, fl
+
+
+# ------------------------------------------------------ reference harness --
+
+_ref = None
+
+
+def reference_harness():
+    """ctypes handle of oracle/_ref/libref_harness.so with the reference's
+    cubin loaded, or None when the cubin is not available."""
+    global _ref
+    if _ref is None:
+        from . import ref_build
+        cubin, so = ref_build.build()
+        if cubin is None or not os.path.exists(cubin):
+            return None
+        L = C.CDLL(so)
+        L.refh_open.argtypes = [C.c_char_p]
+        L.refh_open.restype = C.c_int
+        L.refh_run.argtypes = [i32, i32, i32, f32, C.c_char, i32, i32, i32, i32, i32, i32, i32, f32, f64, f64, i32, i32,
+                               i64, P, P, P, P, P, P, i64]
+        L.refh_run.restype = C.c_int
+        rc = L.refh_open(cubin.encode())
+        if rc != 0:
+            raise RuntimeError(f"reference cubin could not be loaded (code {rc})")
+        _ref = L
+    return _ref
+
+
+def reference_run(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc,
+                  max_outer=0, want_raw=True):
+    """The reference's own kernels, prerun.cu then mainrun.cu order, for R samples.
+    Returns dict(status, pre_ms, main_ms, outer, start, end, windows)."""
+    L = reference_harness()
+    if L is None:
+        raise RuntimeError("reference cubin not available")
+    t_pre, t_main, outer = C.c_double(), C.c_double(), C.c_longlong()
+    starts = np.zeros(R * I, np.int32)
+    ends = np.zeros(R * I, np.int32)
+    cap = R * I * (4 * X * Y + 1)
+    raw = np.zeros(cap if want_raw else 1, np.float64)
+    st = L.refh_run(X, Y, boundary, C.c_float(prob), cls.encode(), seed, R, pre_w, pre_i, pre_n, I, W,
+                    C.c_float(overlap), alpha, beta, n_iter, xc, max_outer, C.byref(t_pre), C.byref(t_main),
+                    C.byref(outer), ptr(starts), ptr(ends), ptr(raw) if want_raw else None, cap)
+    wins = []
+    if want_raw and st == 0:
+        pos = 0
+        for q in range(R * I):
+            ln = int(ends[q] - starts[q] + 1)
+            wins.append(raw[pos:pos + ln].copy())
+            pos += ln
+    return dict(status=st, pre_ms=t_pre.value, main_ms=t_main.value, outer=outer.value, start=starts, end=ends,
+                windows=wins)

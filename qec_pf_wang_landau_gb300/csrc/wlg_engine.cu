@@ -165,16 +165,19 @@ struct Team {
   }
 };
 
-// Site of a draw: trunc(double(u) * ((N-1) + 0.999999)) (wl.cu:63-65),
-// computed in FP32 unless the product lies within site_eps (= N*2^-21, four
-// times the FP32 error bound) of an integer.
+// Site of a draw: trunc(double(u) * ((N-1) + 0.999999)) (wl.cu:63-65).  With
+// f = x / 2^32 the reference's product lies within N*2^-23 + 1e-6 of f*N, so
+// floor(f*N) = umulhi(x, N) is exact unless the fraction x*N mod 2^32 lies
+// within site_thr (= 2^32 (N 2^-21 + 2^-18), >= 4x that bound) of an
+// integer; there the reference's own float/double expression decides.  No
+// int<->float conversion on the common path (they share GB300's slow FP64
+// pipe).
 __device__ __forceinline__ int pick_site(uint32_t x, const MainDesc& d)
 {
-  const float uf = unit_float(x);
-  const float pr = uf * d.site_scale_f;
-  int s = static_cast<int>(pr);
-  const float fr = pr - static_cast<float>(s);
-  if (fr < d.site_eps || fr > 1.0f - d.site_eps) s = static_cast<int>(trunc(static_cast<double>(uf) * d.site_scale));
+  const uint32_t n = static_cast<uint32_t>(d.N);
+  const uint32_t lo = x * n;
+  int s = static_cast<int>(__umulhi(x, n));
+  if (lo < d.site_thr || lo > ~d.site_thr) s = static_cast<int>(trunc(static_cast<double>(unit_float(x)) * d.site_scale));
   return s;
 }
 
@@ -391,7 +394,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       double g_cur = G[c_cur * P + t];
       float gfb = Gf[c_cur * P + t];  // float of g_cur at the last change of bin
       uint32_t h_cur = H[c_cur * P + t];
-      int k = 0;                      // ln f increments since then
+      float kf = 0.0f;                // ln f increments since then (exact below 2^24)
       uint64_t pos = rng.pos;
       uint64_t blk = pos >> 2;
       uint4 A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), rng.s0, rng.s1, rng.k0, rng.k1);
@@ -424,20 +427,23 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const float gfn = Gf[c_new * P + t];
         // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) from FP32 values
         // with a proven error bound eps on the exponent; the reference's FP64
-        // expression decides whenever the bound does not.
-        const float u2 = unit_float(x2);
-        const float kl = static_cast<float>(k) * lnf_f;
+        // expression decides whenever the bound does not.  For a
+        // non-negative exponent the test is u < 1, i.e. x2 < 2^32 - 128
+        // exactly; otherwise u is approximated without a conversion as
+        // (x2 >> 9) 2^-23 (error < 2^-22, margin 2^-21).
+        const float kl = kf * lnf_f;
         const float df = (gfb - gfn) + kl;
         const float eps = 0x1p-22f * (gfb + gfn + kl + fabsf(df));
         const bool nonneg = same || df - eps >= 0.0f;
         const float e = __expf(df);
         const float r = 1.1f * (eps + (2.0f + 1.2f * fabsf(df)) * 0x1p-23f) + 0x1p-22f;
         const float t_lo = e * (1.0f - r), t_hi = e * (1.0f + r);
-        bool acc = nonneg ? (u2 < 1.0f) : (u2 < t_lo);
-        const bool known = nonneg || (df + eps < 0.0f && (u2 < t_lo || u2 >= t_hi));
+        const float ua = __int_as_float(0x3F800000u | (x2 >> 9)) - 1.0f;
+        bool acc = nonneg ? (x2 < 0xFFFFFF80u) : (ua + 0x1p-21f < t_lo);
+        const bool known = nonneg || (df + eps < 0.0f && (ua + 0x1p-21f < t_lo || ua - 0x1p-21f >= t_hi));
         if (inside && !known) {
           const double gn = G[c_new * P + t];
-          acc = static_cast<double>(u2) < fmin(1.0, exp(g_cur - gn));
+          acc = static_cast<double>(unit_float(x2)) < fmin(1.0, exp(g_cur - gn));
         }
         if (bad) {  // wl.cu:1091-1104: a new energy stops the problem
           ++pos;
@@ -457,12 +463,12 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
             g_cur = G[c_new * P + t];
             h_cur = H[c_new * P + t];
             gfb = gfn;
-            k = 0;
+            kf = 0.0f;
             c_cur = c_new;
           }
           g_cur += lnf;
           h_cur += 1u;
-          ++k;
+          kf += 1.0f;
         } else if (change) {
           g_cur = G[c_new * P + t];
           gfb = gfn;

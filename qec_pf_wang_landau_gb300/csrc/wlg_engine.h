@@ -49,7 +49,7 @@ struct MainDesc {
   uint32_t key_wl;               // Philox key of the WL sweeps (wl.cu:1074)
   uint64_t key_ex;               // Philox key of the exchange (wl.cu:796, :875)
   uint32_t site_magic;           // ceil(2^20 / Y): site / Y = site * magic >> 20
-  float site_scale_f, site_eps;
+  uint32_t site_thr;             // 2^32 * (N 2^-21 + 2^-18): site pick needs the exact path within this
   double site_scale;             // (N - 1) + 0.999999, wl.cu:64
   long long max_outer;           // 0 = no cap
   int nwL;                       // 32-bit words per lattice

@@ -454,8 +454,7 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
       if (static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20) != site / q.Y) ok = false;
     if (!ok) return fail(ctx, WLG_ERR_INVALID, "lattice too large for the site division");
     d.site_scale = (N - 1 + 0.999999);
-    d.site_scale_f = static_cast<float>(d.site_scale);
-    d.site_eps = static_cast<float>(N) * 0x1p-21f;
+    d.site_thr = static_cast<uint32_t>(N) * 2048u + 16384u;
     d.max_outer = q.max_outer;
     d.nwL = nwL;
     const int nbins = (e_hi - e_lo) / g + 1;

@@ -34,9 +34,22 @@ __global__ void k_sqrt_chain(double x0, int n, double* f, double* lf)
   }
 }
 
+__global__ void k_fast_exp(const float* x, float* y, int n)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) y[q] = __expf(x[q]);
+}
+
 }  // namespace
 
 extern "C" {
+
+int probe_fast_exp(const float* d_x, float* d_y, int n)
+{
+  k_fast_exp<<<(n + 127) / 128, 128>>>(d_x, d_y, n);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
 
 int probe_curand_uniform(const unsigned long long* d_seeds, const unsigned long long* d_subseqs,
                          const unsigned long long* d_offsets, int n_triples, int n_draws, float* d_out)

@@ -340,3 +340,32 @@ def test_replica_exchange_flat_log_g_swaps_by_permutation(cuda):
             t = b * W + w
             o = (b + 1) * W + perm[t]
             assert got_off[t] == off_lat[o] and got_off[o] == off_lat[t]
+
+
+def test_fast_exp_within_bound_used_by_acceptance(cuda, probe):
+    """The engine's FP32 acceptance test assumes |__expf(x) / exp(x) - 1| <= (2 + 1.2|x|) 2^-23
+    for normal results; checked on a dense grid of [-87, 0]."""
+    torch = cuda
+    x = np.concatenate([np.linspace(-87.0, 0.0, 2_000_001, dtype=np.float32),
+                        -np.logspace(-30, 1, 100_001).astype(np.float32)])
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.zeros_like(dx)
+    probe.probe_fast_exp.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    assert probe.probe_fast_exp(_dptr(dx), _dptr(dy), len(x)) == 0
+    y = dy.cpu().numpy().astype(np.float64)
+    ex = np.exp(x.astype(np.float64))
+    ok = ex > 1.2e-38
+    rel = np.abs(y[ok] / ex[ok] - 1.0)
+    bound = (2.0 + 1.2 * np.abs(x[ok].astype(np.float64))) * 2.0 ** -23
+    assert (rel <= bound).all(), float((rel / bound).max())
+
+
+def test_device_exp_of_nonnegative_is_at_least_one(cuda, probe):
+    """min(1, exp(d)) == 1 for every d >= 0 (the acceptance shortcut for d >= 0)."""
+    torch = cuda
+    x = np.concatenate([[0.0], np.logspace(-320, 2, 20001)])
+    dx = torch.from_numpy(x).cuda()
+    de = torch.zeros_like(dx)
+    dl = torch.zeros_like(dx)
+    assert probe.probe_exp_log(_dptr(dx), _dptr(de), _dptr(dl), len(x)) == 0
+    assert (de.cpu().numpy() >= 1.0).all()
