@@ -19,8 +19,8 @@
 //     over energies the lattice can reach (every 2nd or 4th value);
 //   * the current bin's log g and count cached in registers, written back
 //     only when the walker changes energy.
-// Acceptance min(1, exp(dlogg)) is decided with an FP32 exp and a guard band
-// (1e-5 relative, >6x the worst FP32 error for |dlogg| < 23); inside the
+// Acceptance min(1, exp(dlogg)) is decided with FP32 values and a proven
+// error bound on the exponent (float shadows of log g, __expf); inside the
 // band, and for the site pick near a bin edge, the exact FP64 expression of
 // the reference decides, so every decision equals the reference's.
 
@@ -39,7 +39,6 @@ namespace wlg {
 namespace {
 
 constexpr double kE = 2.718281828459045;  // std::numbers::e, mainrun.cu:56
-constexpr float kBand = 1e-5f;
 
 // ------------------------------------------------------------ pre-run -----
 

@@ -209,12 +209,15 @@ struct DevBuf {
   size_t cap = 0;
 };
 
+// Device buffers of one batch, by role.
+enum Slot { kPreDesc, kJ8, kSeen, kFound, kFflag, kMainDesc, kOrder, kNext, kJw, kLatw, kWin, kMask, kOut, kRes, kSlots };
+
 struct wlg_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   size_t budget = 0;
   size_t used = 0;
-  DevBuf pre_desc, J8, seen, found, fflag, main_desc, order, next, Jw, latw, win, mask, out, res, dump;
+  DevBuf buf[kSlots];
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float t_pre = 0, t_main = 0;
   double t_handoff = 0, t_stitch = 0;
@@ -229,13 +232,29 @@ using wlg::MainDesc;
 using wlg::MainResult;
 using wlg::PreDesc;
 
-wlg_status fail(wlg_context* ctx, wlg_status st, const std::string& msg)
+// Where a batch runs: its stream, a provider of device buffers, optional
+// timing events, and what it did.
+struct Exec {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t* ev = nullptr;  // 4 events, or nullptr for no timing
+  float t_pre = 0, t_main = 0;
+  double t_handoff = 0;
+  long long h2d = 0, d2h = 0;
+  int launches = 0;
+  std::string err;
+  virtual ~Exec() = default;
+  // device buffer for `slot` of at least `bytes` bytes
+  virtual wlg_status buffer(Slot slot, size_t bytes, void** out) = 0;
+};
+
+wlg_status fail(Exec& ex, wlg_status st, const std::string& msg)
 {
-  ctx->err = msg;
+  ex.err = msg;
   return st;
 }
 
-wlg_status grow(wlg_context* ctx, DevBuf& b, size_t bytes)
+wlg_status grow(wlg_context* ctx, DevBuf& b, size_t bytes, std::string& err)
 {
   if (bytes <= b.cap) return WLG_OK;
   bytes = std::max<size_t>(bytes, 256);
@@ -245,32 +264,55 @@ wlg_status grow(wlg_context* ctx, DevBuf& b, size_t bytes)
     b.p = nullptr;
     b.cap = 0;
   }
-  if (ctx->budget != 0 && ctx->used + bytes > ctx->budget) return fail(ctx, WLG_ERR_OOM, "device memory budget");
+  if (ctx->budget != 0 && ctx->used + bytes > ctx->budget) {
+    err = "device memory budget";
+    return WLG_ERR_OOM;
+  }
   const cudaError_t e = cudaMalloc(&b.p, bytes);
-  if (e != cudaSuccess) return fail(ctx, wlg::cuda_status(e), cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    err = cudaGetErrorString(e);
+    return wlg::cuda_status(e);
+  }
   b.cap = bytes;
   ctx->used += bytes;
   return WLG_OK;
 }
 
+// The context's buffers grow on demand and are kept between batches.
+struct ContextExec final : Exec {
+  wlg_context* ctx;
+  explicit ContextExec(wlg_context* c) : ctx(c)
+  {
+    device = c->device;
+    stream = c->stream;
+    ev = c->ev;
+  }
+  wlg_status buffer(Slot slot, size_t bytes, void** out) override
+  {
+    const wlg_status st = grow(ctx, ctx->buf[slot], bytes, err);
+    *out = ctx->buf[slot].p;
+    return st;
+  }
+};
+
 template <typename T>
-wlg_status upload(wlg_context* ctx, DevBuf& b, const std::vector<T>& h)
+wlg_status upload(Exec& ex, Slot slot, const std::vector<T>& h, void** dptr)
 {
   const size_t bytes = h.size() * sizeof(T);
-  wlg_status st = grow(ctx, b, bytes);
+  wlg_status st = ex.buffer(slot, bytes, dptr);
   if (st != WLG_OK || bytes == 0) return st;
-  const cudaError_t e = cudaMemcpyAsync(b.p, h.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
-  ctx->h2d += static_cast<long long>(bytes);
-  return e == cudaSuccess ? WLG_OK : fail(ctx, WLG_ERR_CUDA, cudaGetErrorString(e));
+  const cudaError_t e = cudaMemcpyAsync(*dptr, h.data(), bytes, cudaMemcpyHostToDevice, ex.stream);
+  ex.h2d += static_cast<long long>(bytes);
+  return e == cudaSuccess ? WLG_OK : fail(ex, WLG_ERR_CUDA, cudaGetErrorString(e));
 }
 
 template <typename T>
-wlg_status download(wlg_context* ctx, const DevBuf& b, std::vector<T>& h)
+wlg_status download(Exec& ex, const void* dptr, std::vector<T>& h)
 {
   if (h.empty()) return WLG_OK;
-  const cudaError_t e = cudaMemcpyAsync(h.data(), b.p, h.size() * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream);
-  ctx->d2h += static_cast<long long>(h.size() * sizeof(T));
-  return e == cudaSuccess ? WLG_OK : fail(ctx, WLG_ERR_CUDA, cudaGetErrorString(e));
+  const cudaError_t e = cudaMemcpyAsync(h.data(), dptr, h.size() * sizeof(T), cudaMemcpyDeviceToHost, ex.stream);
+  ex.d2h += static_cast<long long>(h.size() * sizeof(T));
+  return e == cudaSuccess ? WLG_OK : fail(ex, WLG_ERR_CUDA, cudaGetErrorString(e));
 }
 
 int round32(int x) { return (x + 31) / 32 * 32; }
@@ -297,17 +339,17 @@ struct Prepared {
 };
 
 // The whole batch up to the main-run results.
-wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_result* results,
+wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results,
                      std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
                      std::vector<int>& win_host)
 {
   using clock = std::chrono::steady_clock;
-  ctx->h2d = ctx->d2h = 0;
-  ctx->launches = 0;
-  ctx->t_pre = ctx->t_main = 0;
-  ctx->t_handoff = ctx->t_stitch = 0;
+  ex.h2d = ex.d2h = 0;
+  ex.launches = 0;
+  ex.t_pre = ex.t_main = 0;
+  ex.t_handoff = 0;
   for (int p = 0; p < n; ++p) {
-    if (check_problem(probs[p]) != WLG_OK) return fail(ctx, WLG_ERR_INVALID, "invalid problem " + std::to_string(p));
+    if (check_problem(probs[p]) != WLG_OK) return fail(ex, WLG_ERR_INVALID, "invalid problem " + std::to_string(p));
     std::memset(&results[p], 0, sizeof(wlg_result));
   }
   // ---------------- pre-run
@@ -330,7 +372,7 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     std::vector<int> s, e;
     // prerun.cu:23-25: coarse bins of [-2N, 2N] with overlap 1
     if (wlg::make_windows(-2 * d.N, 2 * d.N, q.pre_intervals, 1.0F, s, e) != WLG_OK)
-      return fail(ctx, WLG_ERR_INVALID, "pre-run intervals produce empty bins");
+      return fail(ex, WLG_ERR_INVALID, "pre-run intervals produce empty bins");
     d.len_int = e[0] - s[0] + 1;
     d.n_iter = q.pre_iterations;
     d.off_J = oJ;
@@ -346,30 +388,31 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     threads = std::max(threads, round32(d.walkers));
     results[p].pre_flips = static_cast<long long>(q.pre_walkers) * q.pre_iterations;
   }
-  if (smem > 227 * 1024) return fail(ctx, WLG_ERR_INVALID, "pre-run walkers x lattice too large for shared memory");
+  if (smem > 227 * 1024) return fail(ex, WLG_ERR_INVALID, "pre-run walkers x lattice too large for shared memory");
   wlg_status st;
-  if ((st = upload(ctx, ctx->pre_desc, pd)) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->J8, static_cast<size_t>(oJ))) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->seen, static_cast<size_t>(oS))) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->found, static_cast<size_t>(oF))) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->fflag, static_cast<size_t>(oG) * sizeof(int))) != WLG_OK) return st;
-  cudaMemsetAsync(ctx->found.p, 0, static_cast<size_t>(oF), ctx->stream);
-  cudaEventRecord(ctx->ev[0], ctx->stream);
-  st = wlg::launch_pre_batch(static_cast<const PreDesc*>(ctx->pre_desc.p), n, threads, smem,
-                             static_cast<int8_t*>(ctx->J8.p), static_cast<uint8_t*>(ctx->seen.p),
-                             static_cast<int8_t*>(ctx->found.p), static_cast<int*>(ctx->fflag.p), ctx->stream);
-  if (st != WLG_OK) return fail(ctx, st, "pre-run launch failed");
-  ++ctx->launches;
-  cudaEventRecord(ctx->ev[1], ctx->stream);
+  void *d_pd = nullptr, *d_J8 = nullptr, *d_seen = nullptr, *d_found = nullptr, *d_fflag = nullptr;
+  if ((st = upload(ex, kPreDesc, pd, &d_pd)) != WLG_OK) return st;
+  if ((st = ex.buffer(kJ8, static_cast<size_t>(oJ), &d_J8)) != WLG_OK) return st;
+  if ((st = ex.buffer(kSeen, static_cast<size_t>(oS), &d_seen)) != WLG_OK) return st;
+  if ((st = ex.buffer(kFound, static_cast<size_t>(oF), &d_found)) != WLG_OK) return st;
+  if ((st = ex.buffer(kFflag, static_cast<size_t>(oG) * sizeof(int), &d_fflag)) != WLG_OK) return st;
+  cudaMemsetAsync(d_found, 0, static_cast<size_t>(oF), ex.stream);
+  if (ex.ev != nullptr) cudaEventRecord(ex.ev[0], ex.stream);
+  st = wlg::launch_pre_batch(static_cast<const PreDesc*>(d_pd), n, threads, smem, static_cast<int8_t*>(d_J8),
+                             static_cast<uint8_t*>(d_seen), static_cast<int8_t*>(d_found), static_cast<int*>(d_fflag),
+                             ex.stream);
+  if (st != WLG_OK) return fail(ex, st, "pre-run launch failed");
+  ++ex.launches;
+  if (ex.ev != nullptr) cudaEventRecord(ex.ev[1], ex.stream);
   std::vector<int8_t> J8(static_cast<size_t>(oJ)), found(static_cast<size_t>(oF));
   std::vector<uint8_t> seen(static_cast<size_t>(oS));
   std::vector<int> fflag(static_cast<size_t>(oG));
-  download(ctx, ctx->J8, J8);
-  download(ctx, ctx->seen, seen);
-  download(ctx, ctx->found, found);
-  download(ctx, ctx->fflag, fflag);
-  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, WLG_ERR_CUDA, "pre-run failed");
-  cudaEventElapsedTime(&ctx->t_pre, ctx->ev[0], ctx->ev[1]);
+  download(ex, d_J8, J8);
+  download(ex, d_seen, seen);
+  download(ex, d_found, found);
+  download(ex, d_fflag, fflag);
+  if (cudaStreamSynchronize(ex.stream) != cudaSuccess) return fail(ex, WLG_ERR_CUDA, "pre-run failed");
+  if (ex.ev != nullptr) cudaEventElapsedTime(&ex.t_pre, ex.ev[0], ex.ev[1]);
 
   // ---------------- hand-off (file_io.cpp:558-659, mainrun.cu:79-113)
   const auto t0 = clock::now();
@@ -452,7 +495,7 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     d.site_magic = static_cast<uint32_t>(((1u << 20) + q.Y - 1) / q.Y);
     for (int site = 0; site < N; ++site)
       if (static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20) != site / q.Y) ok = false;
-    if (!ok) return fail(ctx, WLG_ERR_INVALID, "lattice too large for the site division");
+    if (!ok) return fail(ex, WLG_ERR_INVALID, "lattice too large for the site division");
     d.site_scale = (N - 1 + 0.999999);
     d.site_thr = static_cast<uint32_t>(N) * 2048u + 16384u;
     d.max_outer = q.max_outer;
@@ -484,7 +527,7 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     for (int b = 0; b < d.I; ++b) {
       const int8_t* src = found.data() + a.off_found + static_cast<long long>(pick[b]) * N;
       if (wlg::energy_host(src, J8.data() + a.off_J, q.X, q.Y, q.boundary) != E0[b])
-        return fail(ctx, WLG_ERR_ENERGY_RANGE, "stored lattice energy mismatch");
+        return fail(ex, WLG_ERR_ENERGY_RANGE, "stored lattice energy mismatch");
       for (int wd = 0; wd < nwL; ++wd) {
         uint32_t v = 0;
         for (int bit = 0; bit < 32; ++bit) {
@@ -516,19 +559,16 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     prep.main_problem.push_back(p);
     prep.lg.push_back(lg);
   }
-  ctx->t_handoff = std::chrono::duration<double, std::milli>(clock::now() - t0).count();
+  ex.t_handoff = std::chrono::duration<double, std::milli>(clock::now() - t0).count();
 
   // ---------------- main run: one persistent launch per (lattice storage, team size)
   const int m = static_cast<int>(prep.main.size());
   mres.assign(static_cast<size_t>(m), MainResult{});
   out_host.assign(static_cast<size_t>(o_out), 0.0);
   win_host = win;
-  if (m == 0) {
-    ctx->t_main = 0;
-    return WLG_OK;
-  }
+  if (m == 0) return WLG_OK;
   int sms = 1;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ex.device);
   // variant: 0 spins in shared memory, 1 spins in a register, 2 register
   // spins + neighbour table (4 distinct neighbours: X, Y >= 3)
   auto variant_of = [](const MainDesc& d) { return d.N > 64 ? 0 : (d.X >= 3 && d.Y >= 3 ? 2 : 1); };
@@ -546,7 +586,7 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
                        wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, variant != 0, variant == 2 ? d.N : 0).bytes + 16);
     }
     bytes = wlg::align16(bytes);
-    if (bytes > 227 * 1024) return fail(ctx, WLG_ERR_INVALID, "problem state exceeds shared memory");
+    if (bytes > 227 * 1024) return fail(ex, WLG_ERR_INVALID, "problem state exceeds shared memory");
     int per_cta = team <= 256 ? 256 / team : 1;
     per_cta = std::min(per_cta, (227 * 1024) / bytes);
     if (team > 32) per_cta = std::min(per_cta, 15);
@@ -557,36 +597,37 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
     launches.emplace_back(variant, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()));
     order.insert(order.end(), idx.begin(), idx.end());
   }
-  if ((st = upload(ctx, ctx->main_desc, prep.main)) != WLG_OK) return st;
-  if ((st = upload(ctx, ctx->order, order)) != WLG_OK) return st;
-  if ((st = upload(ctx, ctx->Jw, Jw)) != WLG_OK) return st;
-  if ((st = upload(ctx, ctx->latw, latw)) != WLG_OK) return st;
-  if ((st = upload(ctx, ctx->win, win)) != WLG_OK) return st;
-  if ((st = upload(ctx, ctx->mask, maskw)) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->out, static_cast<size_t>(o_out) * sizeof(double))) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->res, static_cast<size_t>(m) * sizeof(MainResult))) != WLG_OK) return st;
-  if ((st = grow(ctx, ctx->next, launches.size() * sizeof(int))) != WLG_OK) return st;
-  cudaMemsetAsync(ctx->next.p, 0, launches.size() * sizeof(int), ctx->stream);
-  cudaEventRecord(ctx->ev[2], ctx->stream);
+  void *d_md = nullptr, *d_order = nullptr, *d_Jw = nullptr, *d_latw = nullptr, *d_win = nullptr, *d_mask = nullptr;
+  void *d_out = nullptr, *d_res = nullptr, *d_next = nullptr;
+  if ((st = upload(ex, kMainDesc, prep.main, &d_md)) != WLG_OK) return st;
+  if ((st = upload(ex, kOrder, order, &d_order)) != WLG_OK) return st;
+  if ((st = upload(ex, kJw, Jw, &d_Jw)) != WLG_OK) return st;
+  if ((st = upload(ex, kLatw, latw, &d_latw)) != WLG_OK) return st;
+  if ((st = upload(ex, kWin, win, &d_win)) != WLG_OK) return st;
+  if ((st = upload(ex, kMask, maskw, &d_mask)) != WLG_OK) return st;
+  if ((st = ex.buffer(kOut, static_cast<size_t>(o_out) * sizeof(double), &d_out)) != WLG_OK) return st;
+  if ((st = ex.buffer(kRes, static_cast<size_t>(m) * sizeof(MainResult), &d_res)) != WLG_OK) return st;
+  if ((st = ex.buffer(kNext, launches.size() * sizeof(int), &d_next)) != WLG_OK) return st;
+  cudaMemsetAsync(d_next, 0, launches.size() * sizeof(int), ex.stream);
+  if (ex.ev != nullptr) cudaEventRecord(ex.ev[2], ex.stream);
   for (size_t g = 0; g < launches.size(); ++g) {
     const auto [variant, team, bytes, per_cta, first, count] = launches[g];
     const int cap = wlg::main_batch_capacity(variant, team * per_cta, bytes * per_cta);
-    if (cap <= 0) return fail(ctx, WLG_ERR_CUDA, "main-run configuration does not fit an SM");
+    if (cap <= 0) return fail(ex, WLG_ERR_CUDA, "main-run configuration does not fit an SM");
     const int grid = std::min(cap, (count + per_cta - 1) / per_cta);
-    st = wlg::launch_main_batch(variant, static_cast<const MainDesc*>(ctx->main_desc.p),
-                                static_cast<const int*>(ctx->order.p) + first, count, team, bytes, per_cta, grid,
-                                static_cast<int*>(ctx->next.p) + g, static_cast<const uint32_t*>(ctx->Jw.p),
-                                static_cast<const uint32_t*>(ctx->latw.p), static_cast<const int*>(ctx->win.p),
-                                static_cast<const uint32_t*>(ctx->mask.p), static_cast<double*>(ctx->out.p),
-                                static_cast<MainResult*>(ctx->res.p), nullptr, ctx->stream);
-    if (st != WLG_OK) return fail(ctx, st, "main-run launch failed");
-    ++ctx->launches;
+    st = wlg::launch_main_batch(variant, static_cast<const MainDesc*>(d_md), static_cast<const int*>(d_order) + first,
+                                count, team, bytes, per_cta, grid, static_cast<int*>(d_next) + g,
+                                static_cast<const uint32_t*>(d_Jw), static_cast<const uint32_t*>(d_latw),
+                                static_cast<const int*>(d_win), static_cast<const uint32_t*>(d_mask),
+                                static_cast<double*>(d_out), static_cast<MainResult*>(d_res), nullptr, ex.stream);
+    if (st != WLG_OK) return fail(ex, st, "main-run launch failed");
+    ++ex.launches;
   }
-  cudaEventRecord(ctx->ev[3], ctx->stream);
-  download(ctx, ctx->res, mres);
-  download(ctx, ctx->out, out_host);
-  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, WLG_ERR_CUDA, "main run failed");
-  cudaEventElapsedTime(&ctx->t_main, ctx->ev[2], ctx->ev[3]);
+  if (ex.ev != nullptr) cudaEventRecord(ex.ev[3], ex.stream);
+  download(ex, d_res, mres);
+  download(ex, d_out, out_host);
+  if (cudaStreamSynchronize(ex.stream) != cudaSuccess) return fail(ex, WLG_ERR_CUDA, "main run failed");
+  if (ex.ev != nullptr) cudaEventElapsedTime(&ex.t_main, ex.ev[2], ex.ev[3]);
   for (int i = 0; i < m; ++i) {
     wlg_result& r = results[prep.main_problem[i]];
     r.status = mres[i].status;
@@ -596,6 +637,22 @@ wlg_status run_batch(wlg_context* ctx, const wlg_problem* probs, int n, wlg_resu
   }
   return WLG_OK;
 }
+
+void keep_stats(wlg_context* ctx, const Exec& ex)
+{
+  ctx->t_pre = ex.t_pre;
+  ctx->t_main = ex.t_main;
+  ctx->t_handoff = ex.t_handoff;
+  ctx->t_stitch = 0;
+  ctx->h2d = ex.h2d;
+  ctx->d2h = ex.d2h;
+  ctx->launches = ex.launches;
+  if (!ex.err.empty()) ctx->err = ex.err;
+}
+
+wlg_status raw_windows(Exec& ex, const wlg_problem* problems, int n, const Prepared& prep,
+                       const std::vector<double>& out, const std::vector<int>& win, int* win_start, int* win_end,
+                       double* raw_log_g, long long raw_capacity, long long* raw_offset);
 
 // Dense walker-0 log g of window b (zeros where the lattice cannot reach).
 void dense_window(const MainDesc& d, const std::vector<double>& out, const std::vector<int>& win, int b,
@@ -635,9 +692,8 @@ wlg_status wlg_context_destroy(wlg_context* ctx)
   if (ctx == nullptr) return WLG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->pre_desc, &ctx->J8, &ctx->seen, &ctx->found, &ctx->fflag, &ctx->main_desc, &ctx->order,
-                    &ctx->next, &ctx->Jw, &ctx->latw, &ctx->win, &ctx->mask, &ctx->out, &ctx->res, &ctx->dump})
-    if (b->p != nullptr) cudaFree(b->p);
+  for (DevBuf& b : ctx->buf)
+    if (b.p != nullptr) cudaFree(b.p);
   for (auto& e : ctx->ev) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -655,8 +711,22 @@ wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, w
   Prepared prep;
   std::vector<double> out;
   std::vector<int> win;
-  wlg_status st = run_batch(ctx, problems, n, results, mres, prep, out, win);
+  ContextExec ex(ctx);
+  wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
+  keep_stats(ctx, ex);
   if (st != WLG_OK) return st;
+  return raw_windows(ex, problems, n, prep, out, win, win_start, win_end, raw_log_g, raw_capacity, raw_offset);
+}
+
+}  // extern "C"
+
+namespace {
+
+// The walker-0 log g of every window on the reference's dense layout.
+wlg_status raw_windows(Exec& ex, const wlg_problem* problems, int n, const Prepared& prep,
+                       const std::vector<double>& out, const std::vector<int>& win, int* win_start, int* win_end,
+                       double* raw_log_g, long long raw_capacity, long long* raw_offset)
+{
   long long pos = 0;
   std::vector<int> slot(static_cast<size_t>(n), -1);
   for (size_t i = 0; i < prep.main.size(); ++i) slot[prep.main_problem[i]] = static_cast<int>(i);
@@ -675,13 +745,17 @@ wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, w
     std::vector<double> dense;
     for (int b = 0; b < d.I; ++b) {
       dense_window(d, out, win, b, dense);
-      if (pos + static_cast<long long>(dense.size()) > raw_capacity) return fail(ctx, WLG_ERR_CAPACITY, "raw output");
+      if (pos + static_cast<long long>(dense.size()) > raw_capacity) return fail(ex, WLG_ERR_CAPACITY, "raw output");
       if (raw_log_g != nullptr) std::memcpy(raw_log_g + pos, dense.data(), dense.size() * sizeof(double));
       pos += static_cast<long long>(dense.size());
     }
   }
   return WLG_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* energies,
                      double* log_g, long long capacity)
@@ -692,7 +766,9 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
   Prepared prep;
   std::vector<double> out;
   std::vector<int> win;
-  wlg_status st = run_batch(ctx, problems, n, results, mres, prep, out, win);
+  ContextExec ex(ctx);
+  wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
+  keep_stats(ctx, ex);
   if (st != WLG_OK) return st;
   const auto t0 = std::chrono::steady_clock::now();
   long long pos = 0;
@@ -717,7 +793,10 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
       r.status = sst;
       continue;
     }
-    if (pos + static_cast<long long>(res.size()) > capacity) return fail(ctx, WLG_ERR_CAPACITY, "result arrays");
+    if (pos + static_cast<long long>(res.size()) > capacity) {
+      ctx->err = "result arrays";
+      return WLG_ERR_CAPACITY;
+    }
     for (size_t k = 0; k < res.size(); ++k) {
       energies[pos + static_cast<long long>(k)] = res[k].first;
       log_g[pos + static_cast<long long>(k)] = res[k].second;

@@ -48,19 +48,27 @@ def test_reference_kernels_match_exact_enumeration_4x4(ref):
         assert np.sqrt(np.mean(err ** 2)) < 0.25
 
 
-def test_engine_and_reference_agree_within_wl_tolerance_6x6(ref):
+def test_engine_error_not_worse_than_reference_6x6(ref):
+    """6x6 periodic, class v, the reference's flags (exchange off as in its loop):
+    both log g curves against the exact transfer-matrix density of states; the
+    engine's error must be of the reference's size or smaller."""
     import qec_pf_wang_landau_gb300 as wlg
     R, I = 4, 10
     out = O.reference_run(6, 6, 0, 0.04, "v", 777, R, 128, 32, 1000, I, 3, 0.25, 0.8, 1e-3, 1000, 20)
     assert out["status"] == 0
     probs = [wlg.problem(6, 6, prob=0.04, error_class="v", seed=777, sample=k, exchange_mode=0) for k in range(R)]
     mine = wlg.Context(0).solve(probs)
+    J = O.init_interactions(6, 6, R, 777, 0.04, "v")
+    e_ref, e_mine = [], []
     for k in range(R):
         E, G = _stitch(out["windows"][k * I:(k + 1) * I], out["start"][k * I:(k + 1) * I],
                        out["end"][k * I:(k + 1) * I], 6, 6)
         r, E2, G2 = mine[k]
         assert r.status == 0
-        common = np.intersect1d(E, E2)
-        assert len(common) >= 0.9 * max(len(E), len(E2))
-        d = G[np.searchsorted(E, common)] - G2[np.searchsorted(E2, common)]
-        assert np.sqrt(np.mean(d ** 2)) < 0.3
+        cnt = O.exact_counts(J[k * 72:(k + 1) * 72], 6, 6, 0)
+        exact_E = set((np.nonzero(cnt)[0] - 72).tolist())
+        assert set(E2.tolist()) == exact_E
+        e_ref.append(np.sqrt(np.mean((G - np.log(cnt[E + 72])) ** 2)))
+        e_mine.append(np.sqrt(np.mean((G2 - np.log(cnt[E2 + 72])) ** 2)))
+    assert max(e_ref) < 1.0 and max(e_mine) < 1.0
+    assert np.mean(e_mine) < 1.5 * np.mean(e_ref) + 0.1, (e_mine, e_ref)
