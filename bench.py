@@ -81,6 +81,37 @@ def cpu_run(n: int, threads: int):
     return ok / dt, float(fl.sum()) / dt, dt
 
 
+def plain_run():
+    """The plain form (reference structure on this engine's operators) on the
+    same 400 problems: (converged problems/s, seconds, kernel launches)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = problems(0)
+    t0 = time.perf_counter()
+    out, launches = wlg.solve_plain(probs)
+    dt = time.perf_counter() - t0
+    return sum(1 for r, _, _ in out if r.status == 0) / dt, dt, launches
+
+
+def reference_cuda_run():
+    """The reference's own CUDA kernels (unmodified wl.cu, cubin) in its
+    prerun/mainrun order, one run of 100 samples per error class.  Its
+    exchange counter never advances, so at -c 20 it runs without exchange.
+    Returns (converged samples/s, seconds) or None without the cubin."""
+    import oracle as O
+    if O.reference_harness() is None:
+        return None
+    w = WORKLOAD
+    tot_ms, conv = 0.0, 0
+    for c in w["classes"]:
+        out = O.reference_run(w["X"], w["Y"], w["boundary"], w["prob"], c, w["seed"], w["samples"], w["pre_walkers"],
+                              w["pre_intervals"], w["pre_iterations"], w["intervals"], w["walkers_per_interval"],
+                              w["overlap"], w["alpha"], w["beta"], w["iterations"], w["exchange_every"],
+                              want_raw=False)
+        tot_ms += out["pre_ms"] + out["main_ms"]
+        conv += w["samples"] if out["status"] == 0 else 0
+    return conv / (tot_ms / 1e3), tot_ms / 1e3
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -202,6 +233,8 @@ def run_ours(args):
         return None
     peaks, peak_kind = measured_peaks()
     achieved = BYTES_PER_FLIP * flips / max(t_main, 1e-12) / 1e9
+    plain_pps, plain_s, plain_launches = plain_run()
+    ref_cuda = reference_cuda_run()
     cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1)
     line = {
         "metric": METRIC,
@@ -231,6 +264,14 @@ def run_ours(args):
                          "sample": f"{CPU_SAMPLE_PROBLEMS} problems of the same workload (samples 0-23 x ivhc), "
                                    f"{cpu_s:.1f} s wall"},
     }
+    line["plain"] = {"value": plain_pps, "unit": "samples/s", "seconds": plain_s, "kernel_launches": plain_launches,
+                     "what": "same 400 problems, reference structure on this engine's operator kernels "
+                             "(one launch per operation, host loop)"}
+    if ref_cuda is not None:
+        line["reference_cuda"] = {"value": ref_cuda[0], "unit": "samples/s", "seconds": ref_cuda[1],
+                                  "what": "the reference's own kernels (unmodified wl.cu compiled for sm_103a) in its "
+                                          "prerun/mainrun order on this GB300; its exchange counter never "
+                                          "advances, so it runs without replica exchange at -c 20"}
     if clocks is not None:
         line["clocks"] = clocks
     return line

@@ -391,7 +391,15 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       const float lnf_f = static_cast<float>(lnf);
       int c_cur = (E - bb) >> d.lg;
       double g_cur = G[c_cur * P + t];
-      float gfb = Gf[c_cur * P + t];  // float of g_cur at the last change of bin
+      // float shadows of this walker's log g relative to gbase: differences
+      // inside a window stay small while absolute values reach 1e4, so the
+      // relative shadow keeps the FP32 error bound (and the FP64 fallback
+      // rate) small
+      const double gbase = g_cur;
+      for (int c = 0; c < d.L; ++c) Gf[c * P + t] = static_cast<float>(G[c * P + t] - gbase);
+      // one rounding of a double of size |g| <= |gbase| + (small shadow terms)
+      const float ulp_g = static_cast<float>((fabs(gbase) + 1.0) * 0x1p-51);
+      float gfb = 0.0f;               // float of g_cur - gbase at the last change of bin
       uint32_t h_cur = H[c_cur * P + t];
       float kf = 0.0f;                // ln f increments since then (exact below 2^24)
       uint64_t pos = rng.pos;
@@ -432,7 +440,10 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         // (x2 >> 9) 2^-23 (error < 2^-22, margin 2^-21).
         const float kl = kf * lnf_f;
         const float df = (gfb - gfn) + kl;
-        const float eps = 0x1p-22f * (gfb + gfn + kl + fabsf(df));
+        // |df - (g_cur - g_new)|: float roundings of the shadows and of df
+        // (2^-22 = 4x their 2^-24), plus the k sequential double additions in
+        // g_cur and the double differences, each <= one rounding at |g|
+        const float eps = 0x1p-22f * (fabsf(gfb) + fabsf(gfn) + kl + fabsf(df)) + (kf + 4.0f) * ulp_g;
         const bool nonneg = same || df - eps >= 0.0f;
         const float e = __expf(df);
         const float r = 1.1f * (eps + (2.0f + 1.2f * fabsf(df)) * 0x1p-23f) + 0x1p-22f;
@@ -457,7 +468,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         if (!frozen) {
           if (change) {
             G[c_cur * P + t] = g_cur;
-            Gf[c_cur * P + t] = static_cast<float>(g_cur);
+            Gf[c_cur * P + t] = static_cast<float>(g_cur - gbase);
             H[c_cur * P + t] = h_cur;
             g_cur = G[c_new * P + t];
             h_cur = H[c_new * P + t];
@@ -481,7 +492,6 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       }
       if (!frozen) {
         G[c_cur * P + t] = g_cur;
-        Gf[c_cur * P + t] = static_cast<float>(g_cur);
         H[c_cur * P + t] = h_cur;
       }
       rng.pos = pos;
@@ -527,11 +537,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       if (mask_has(mask, ((w_base[wb] - d.e_min) >> d.lg) + c)) {
         for (int v = 0; v < W; ++v) avg += G[c * P + wb * W + v] / W;
       }
-      const float avg_f = static_cast<float>(avg);
-      for (int v = 0; v < W; ++v) {
-        G[c * P + wb * W + v] = avg;
-        Gf[c * P + wb * W + v] = avg_f;
-      }
+      for (int v = 0; v < W; ++v) G[c * P + wb * W + v] = avg;
     }
     team.sync();
     // ---- reset and convergence (wl.cu:596-613, :662-708, mainrun.cu:243, :342-344)
