@@ -222,6 +222,24 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
 wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* win_start,
                          int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset);
 
+/* No counterpart in the reference.  wlg_solve_raw without a context and
+ * without allocating any device memory, for callers that cannot call
+ * cudaMalloc: a framework that owns the device's whole memory pool, a
+ * latency-critical loop that cannot take an allocation's implicit
+ * synchronisation, a deployment that forbids allocating after start-up.
+ * Every device buffer it needs comes from one fixed 8 MiB arena compiled
+ * into the library, which each GPU that loads the library holds until the
+ * process exits.  A batch whose worst-case footprint exceeds the arena is
+ * rejected with WLG_ERR_CAPACITY before anything runs (400 problems of 6x6
+ * lattices fit).  Runs on the current device and `stream`; returns after
+ * the stream has finished the batch.  The first call on a device looks up
+ * the arena's device address, so make that first call before any stream
+ * capture.  All calls share the arena, which keeps the last call's
+ * contents: calls that overlap on the GPU race, so serialise them. */
+wlg_status wlg_solve_raw_noalloc(const wlg_problem* problems, int n, wlg_result* results, int* win_start,
+                                 int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset,
+                                 wlg_stream stream);
+
 /* Plain form: the same problems computed with the reference's own structure
  * (prerun.cu:36-154, mainrun.cu:115-421) on the operators above — one
  * launch per operation, one thread per walker, state in global memory,

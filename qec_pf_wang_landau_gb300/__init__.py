@@ -48,6 +48,7 @@ SIGNATURES = {
     "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
     "wlg_last_stats": [P, P],
     "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
+    "wlg_solve_raw_noalloc": [P, i32, P, P, P, P, i64, P, P],
     "wlg_class_log_probs": [P, P, P, P, i32, f64, P, P],
 }
 _RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p}

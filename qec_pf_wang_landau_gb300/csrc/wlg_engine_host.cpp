@@ -853,3 +853,94 @@ wlg_status wlg_class_log_probs(const int* energies, const double* log_g, const l
 }
 
 }  // extern "C"
+
+// ----------------------------------------------- solve without allocating --
+
+namespace wlg {
+wlg_status noalloc_arena(void** out, size_t* bytes);
+}
+
+namespace {
+
+// Device buffers carved in order out of the fixed arena of wlg_noalloc.cu.
+struct ArenaExec final : Exec {
+  unsigned char* base = nullptr;
+  size_t cap = 0, used = 0;
+  void* slot_ptr[kSlots] = {};
+  size_t slot_cap[kSlots] = {};
+  wlg_status buffer(Slot slot, size_t bytes, void** out) override
+  {
+    if (slot_ptr[slot] != nullptr && slot_cap[slot] >= bytes) {
+      *out = slot_ptr[slot];
+      return WLG_OK;
+    }
+    const size_t off = (used + 255) & ~size_t{255};
+    if (off + bytes > cap) {
+      err = "batch does not fit the " + std::to_string(cap >> 20) + " MiB no-allocation arena";
+      return WLG_ERR_CAPACITY;
+    }
+    slot_ptr[slot] = base + off;
+    slot_cap[slot] = bytes;
+    used = off + bytes;
+    *out = slot_ptr[slot];
+    return WLG_OK;
+  }
+};
+
+// Upper bound of the arena bytes a batch needs, from the problem parameters
+// alone (windows of the full range [-2N, 2N], energy step 2), so oversized
+// batches are rejected before anything runs.
+size_t noalloc_bound(const wlg_problem* probs, int n)
+{
+  auto pad = [](size_t x) { return (x + 255) & ~size_t{255}; };
+  size_t pre_desc = 0, j8 = 0, seen = 0, found = 0, fflag = 0;
+  size_t md = 0, order = 0, jw = 0, latw = 0, win = 0, mask = 0, out = 0, res = 0;
+  for (int p = 0; p < n; ++p) {
+    const wlg_problem& q = probs[p];
+    const size_t N = static_cast<size_t>(q.X) * q.Y, I = static_cast<size_t>(q.intervals);
+    const size_t nwL = (N + 31) / 32, nbins = 2 * N + 1;
+    pre_desc += sizeof(PreDesc);
+    j8 += 2 * N;
+    seen += 4 * N + 1;
+    found += static_cast<size_t>(q.pre_intervals) * N;
+    fflag += 2 * static_cast<size_t>(q.pre_intervals) * sizeof(int);
+    md += sizeof(MainDesc);
+    order += sizeof(int);
+    jw += 2 * nwL * 4;
+    latw += I * nwL * 4;
+    win += 5 * I * sizeof(int);
+    mask += (nbins + 31) / 32 * 4;
+    out += I * nbins * sizeof(double);
+    res += sizeof(MainResult);
+  }
+  return pad(pre_desc) + pad(j8) + pad(seen) + pad(found) + pad(fflag) + pad(md) + pad(order) + pad(jw) + pad(latw) +
+         pad(win) + pad(mask) + pad(out) + pad(res) + pad(64 * sizeof(int));
+}
+
+}  // namespace
+
+extern "C" {
+
+wlg_status wlg_solve_raw_noalloc(const wlg_problem* problems, int n, wlg_result* results, int* win_start,
+                                 int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset,
+                                 wlg_stream stream)
+{
+  if (n < 0 || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+  ArenaExec ex;
+  void* base = nullptr;
+  wlg_status st = wlg::noalloc_arena(&base, &ex.cap);
+  if (st != WLG_OK) return st;
+  ex.base = static_cast<unsigned char*>(base);
+  if (noalloc_bound(problems, n) > ex.cap) return WLG_ERR_CAPACITY;
+  cudaGetDevice(&ex.device);
+  ex.stream = wlg::as_stream(stream);
+  std::vector<MainResult> mres;
+  Prepared prep;
+  std::vector<double> out;
+  std::vector<int> win;
+  st = run_batch(ex, problems, n, results, mres, prep, out, win);
+  if (st != WLG_OK) return st;
+  return raw_windows(ex, problems, n, prep, out, win, win_start, win_end, raw_log_g, raw_capacity, raw_offset);
+}
+
+}  // extern "C"
