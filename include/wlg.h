@@ -253,11 +253,15 @@ wlg_status wlg_solve_plain(const wlg_problem* problems, int n, wlg_result* resul
 /* What the last wlg_solve / wlg_solve_raw did: time by phase in
  * milliseconds (device phases by CUDA events on the context's stream, host
  * phases by the host clock), bytes copied host->device and device->host,
- * and the number of engine kernels launched. */
+ * the number of engine kernels launched, and which main-run kernel forms
+ * ran (bit v for form v: 0 lattice and log g in shared memory, 1 lattice in
+ * registers, 2 lattice in registers with a neighbour table, 3 lattice in
+ * shared memory and FP64 log g in a global pool). */
 typedef struct {
   double pre_ms, handoff_ms, main_ms, stitch_ms;
   long long h2d_bytes, d2h_bytes;
   int kernel_launches;
+  int main_forms;
 } wlg_stats;
 
 wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out);

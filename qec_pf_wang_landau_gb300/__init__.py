@@ -194,7 +194,7 @@ class Context:
 
 class Stats(C.Structure):
     _fields_ = [("pre_ms", f64), ("handoff_ms", f64), ("main_ms", f64), ("stitch_ms", f64), ("h2d_bytes", i64),
-                ("d2h_bytes", i64), ("kernel_launches", i32)]
+                ("d2h_bytes", i64), ("kernel_launches", i32), ("main_forms", i32)]
 
 
 def solve_plain(problems, stream=None):

@@ -266,16 +266,19 @@ __device__ __forceinline__ uint32_t pick_word(const uint4& A, const uint4& B, in
   return v;
 }
 
-template <bool kReg, bool kTable>
-__device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base,
+template <bool kReg, bool kTable, bool kGlobalG>
+__device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base, double* gslot,
                             const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
                             const int* __restrict__ winpool, const uint32_t* __restrict__ maskpool,
                             double* __restrict__ outpool, MainResult* __restrict__ results,
                             uint32_t* __restrict__ dumppool)
 {
   const int P = team.size;
-  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg, kTable ? d.N : 0);
-  double* G = reinterpret_cast<double*>(base + lay.off_G);
+  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg, kTable ? d.N : 0, !kGlobalG);
+  // FP64 log g: in the team's shared memory, or (large problems) in this
+  // resident team's slice of a global pool, L2-resident and touched only on
+  // bin changes, averaging and exchange
+  double* G = kGlobalG ? gslot : reinterpret_cast<double*>(base + lay.off_G);
   float* Gf = reinterpret_cast<float*>(base + lay.off_Gf);
   uint32_t* H = reinterpret_cast<uint32_t*>(base + lay.off_H);
   uint32_t* lat_s = reinterpret_cast<uint32_t*>(base + lay.off_lat);
@@ -650,9 +653,10 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   team.sync();
 }
 
-template <bool kReg, bool kTable, int kMaxThreads>
+template <bool kReg, bool kTable, bool kGlobalG, int kMaxThreads>
 __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __restrict__ descs, const int* __restrict__ order,
                                                      int n, int team_size, int team_bytes, int* __restrict__ next,
+                                                     double* __restrict__ gpool, long long gslot_doubles,
                                                      const uint32_t* __restrict__ Jpool,
                                                      const uint32_t* __restrict__ latpool,
                                                      const int* __restrict__ winpool,
@@ -674,7 +678,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __re
     if (q >= n) return;
     const int p = order[q];
     const MainDesc d = descs[p];
-    run_problem<kReg, kTable>(d, p, team, t, base, Jpool, latpool, winpool, maskpool, outpool, results, dumppool);
+    double* gslot = kGlobalG ? gpool + (static_cast<long long>(blockIdx.x) * (blockDim.x / team_size) + tix) * gslot_doubles
+                             : nullptr;
+    run_problem<kReg, kTable, kGlobalG>(d, p, team, t, base, gslot, Jpool, latpool, winpool, maskpool, outpool, results,
+                                        dumppool);
   }
 }
 
@@ -694,23 +701,28 @@ wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem
   return launch_status();
 }
 
-using MainFn = void (*)(const MainDesc*, const int*, int, int, int, int*, const uint32_t*, const uint32_t*, const int*,
-                        const uint32_t*, double*, MainResult*, uint32_t*);
+using MainFn = void (*)(const MainDesc*, const int*, int, int, int, int*, double*, long long, const uint32_t*,
+                        const uint32_t*, const int*, const uint32_t*, double*, MainResult*, uint32_t*);
 
-// variant: 0 = spins in shared memory, 1 = spins in a register, 2 = register
-// spins + neighbour table
+// variant: 0 = spins and log g in shared memory, 1 = spins in a register,
+// 2 = register spins + neighbour table, 3 = spins in shared memory, FP64 log g
+// in a global pool (problems too large for one SM's shared memory)
+template <int kMaxThreads>
+MainFn main_fn_for(int variant)
+{
+  switch (variant) {
+    case 1: return &k_main_batch<true, false, false, kMaxThreads>;
+    case 2: return &k_main_batch<true, true, false, kMaxThreads>;
+    case 3: return &k_main_batch<false, false, true, kMaxThreads>;
+    default: return &k_main_batch<false, false, false, kMaxThreads>;
+  }
+}
+
 MainFn main_fn(int variant, int cta_threads)
 {
-  if (cta_threads <= 256) {
-    if (variant == 2) return &k_main_batch<true, true, 256>;
-    return variant == 1 ? &k_main_batch<true, false, 256> : &k_main_batch<false, false, 256>;
-  }
-  if (cta_threads <= 512) {
-    if (variant == 2) return &k_main_batch<true, true, 512>;
-    return variant == 1 ? &k_main_batch<true, false, 512> : &k_main_batch<false, false, 512>;
-  }
-  if (variant == 2) return &k_main_batch<true, true, 1024>;
-  return variant == 1 ? &k_main_batch<true, false, 1024> : &k_main_batch<false, false, 1024>;
+  if (cta_threads <= 256) return main_fn_for<256>(variant);
+  if (cta_threads <= 512) return main_fn_for<512>(variant);
+  return main_fn_for<1024>(variant);
 }
 
 // Returns the number of resident CTAs the launch may use (0 if the
@@ -728,7 +740,8 @@ int main_batch_capacity(int variant, int cta_threads, int smem)
 }
 
 wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
-                             int team_bytes, int teams_per_cta, int grid, int* d_next, const uint32_t* Jpool,
+                             int team_bytes, int teams_per_cta, int grid, int* d_next, double* gpool,
+                             long long gslot_doubles, const uint32_t* Jpool,
                              const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
                              MainResult* results, uint32_t* dumppool, cudaStream_t s)
 {
@@ -737,8 +750,8 @@ wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_
   const int smem = team_bytes * teams_per_cta;
   MainFn fn = main_fn(variant, threads);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return WLG_ERR_CUDA;
-  fn<<<grid, threads, smem, s>>>(d_descs, d_order, n, team_size, team_bytes, d_next, Jpool, latpool, winpool,
-                                 maskpool, outpool, results, dumppool);
+  fn<<<grid, threads, smem, s>>>(d_descs, d_order, n, team_size, team_bytes, d_next, gpool, gslot_doubles, Jpool,
+                                 latpool, winpool, maskpool, outpool, results, dumppool);
   return launch_status();
 }
 

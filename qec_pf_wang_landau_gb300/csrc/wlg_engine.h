@@ -80,13 +80,15 @@ struct TeamLayout {
 WLG_HD inline int align16(int x) { return (x + 15) & ~15; }
 
 // reg_lattice: spins in a register (N <= 64); nbt_sites: sites of the
-// neighbour table (0 when the table is not used).
-WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, bool reg_lattice, int nbt_sites)
+// neighbour table (0 when the table is not used); g_in_smem: FP64 log g in
+// shared memory (else in a global pool).
+WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, bool reg_lattice, int nbt_sites,
+                                     bool g_in_smem = true)
 {
   TeamLayout t{};
   int o = 0;
   t.off_G = o;
-  o = align16(o + 8 * L * team);
+  o = align16(o + (g_in_smem ? 8 * L * team : 0));
   t.off_Gf = o;
   o = align16(o + 4 * L * team);
   t.off_H = o;

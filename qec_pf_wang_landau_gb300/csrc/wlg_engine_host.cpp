@@ -28,7 +28,8 @@ wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem
                             int8_t* found_pool, int* fflag_pool, cudaStream_t s);
 int main_batch_capacity(int variant, int cta_threads, int smem);
 wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
-                             int team_bytes, int teams_per_cta, int grid, int* d_next, const uint32_t* Jpool,
+                             int team_bytes, int teams_per_cta, int grid, int* d_next, double* gpool,
+                             long long gslot_doubles, const uint32_t* Jpool,
                              const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
                              MainResult* results, uint32_t* dumppool, cudaStream_t s);
 
@@ -210,7 +211,24 @@ struct DevBuf {
 };
 
 // Device buffers of one batch, by role.
-enum Slot { kPreDesc, kJ8, kSeen, kFound, kFflag, kMainDesc, kOrder, kNext, kJw, kLatw, kWin, kMask, kOut, kRes, kSlots };
+enum Slot {
+  kPreDesc,
+  kJ8,
+  kSeen,
+  kFound,
+  kFflag,
+  kMainDesc,
+  kOrder,
+  kNext,
+  kJw,
+  kLatw,
+  kWin,
+  kMask,
+  kOut,
+  kRes,
+  kGpool,
+  kSlots
+};
 
 struct wlg_context {
   int device = 0;
@@ -223,6 +241,7 @@ struct wlg_context {
   double t_handoff = 0, t_stitch = 0;
   long long h2d = 0, d2h = 0;
   int launches = 0;
+  int main_forms = 0;
   std::string err;
 };
 
@@ -242,6 +261,7 @@ struct Exec {
   double t_handoff = 0;
   long long h2d = 0, d2h = 0;
   int launches = 0;
+  int main_forms = 0;  // bit v: a main-run launch of form v
   std::string err;
   virtual ~Exec() = default;
   // device buffer for `slot` of at least `bytes` bytes
@@ -346,6 +366,7 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
   using clock = std::chrono::steady_clock;
   ex.h2d = ex.d2h = 0;
   ex.launches = 0;
+  ex.main_forms = 0;
   ex.t_pre = ex.t_main = 0;
   ex.t_handoff = 0;
   for (int p = 0; p < n; ++p) {
@@ -575,17 +596,29 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
   std::map<std::pair<int, int>, std::vector<int>> groups;
   for (int i = 0; i < m; ++i) groups[{variant_of(prep.main[i]), prep.main[i].team}].push_back(i);
   std::vector<int> order;
-  std::vector<std::tuple<int, int, int, int, int, int>> launches;  // variant, team, bytes, per_cta, first, count
+  // variant, team, bytes, per_cta, first, count, L (max compact bins)
+  std::vector<std::tuple<int, int, int, int, int, int, int>> launches;
   for (const auto& [key, idx] : groups) {
-    const int variant = key.first;
+    int variant = key.first;
     const int team = key.second;
-    int bytes = 0;
-    for (int i : idx) {
-      const MainDesc& d = prep.main[i];
-      bytes = std::max(bytes,
-                       wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, variant != 0, variant == 2 ? d.N : 0).bytes + 16);
+    auto group_bytes = [&](bool g_in_smem) {
+      int b = 0;
+      for (int i : idx) {
+        const MainDesc& d = prep.main[i];
+        b = std::max(b, wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, variant == 1 || variant == 2,
+                                         variant == 2 ? d.N : 0, g_in_smem)
+                            .bytes +
+                          16);
+      }
+      return wlg::align16(b);
+    };
+    int bytes = group_bytes(true);
+    int Lmax = 1;
+    for (int i : idx) Lmax = std::max(Lmax, prep.main[i].L);
+    if (bytes > 227 * 1024 && variant == 0) {
+      variant = 3;  // FP64 log g moves to a global pool
+      bytes = group_bytes(false);
     }
-    bytes = wlg::align16(bytes);
     if (bytes > 227 * 1024) return fail(ex, WLG_ERR_INVALID, "problem state exceeds shared memory");
     int per_cta = team <= 256 ? 256 / team : 1;
     per_cta = std::min(per_cta, (227 * 1024) / bytes);
@@ -594,7 +627,8 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
     // than packing them into few CTAs
     per_cta = std::min(per_cta, static_cast<int>(idx.size()) / (2 * sms));
     per_cta = std::max(per_cta, 1);
-    launches.emplace_back(variant, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()));
+    launches.emplace_back(variant, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()),
+                          Lmax);
     order.insert(order.end(), idx.begin(), idx.end());
   }
   void *d_md = nullptr, *d_order = nullptr, *d_Jw = nullptr, *d_latw = nullptr, *d_win = nullptr, *d_mask = nullptr;
@@ -609,19 +643,39 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
   if ((st = ex.buffer(kRes, static_cast<size_t>(m) * sizeof(MainResult), &d_res)) != WLG_OK) return st;
   if ((st = ex.buffer(kNext, launches.size() * sizeof(int), &d_next)) != WLG_OK) return st;
   cudaMemsetAsync(d_next, 0, launches.size() * sizeof(int), ex.stream);
-  if (ex.ev != nullptr) cudaEventRecord(ex.ev[2], ex.stream);
+  // grids, and the global log g pool of the variant-3 launches (one slice per
+  // resident team, launches side by side)
+  std::vector<int> grids(launches.size());
+  std::vector<long long> gpool_off(launches.size(), 0);
+  long long gpool_doubles = 0;
   for (size_t g = 0; g < launches.size(); ++g) {
-    const auto [variant, team, bytes, per_cta, first, count] = launches[g];
+    const auto [variant, team, bytes, per_cta, first, count, Lmax] = launches[g];
     const int cap = wlg::main_batch_capacity(variant, team * per_cta, bytes * per_cta);
     if (cap <= 0) return fail(ex, WLG_ERR_CUDA, "main-run configuration does not fit an SM");
-    const int grid = std::min(cap, (count + per_cta - 1) / per_cta);
+    grids[g] = std::min(cap, (count + per_cta - 1) / per_cta);
+    if (variant == 3) {
+      gpool_off[g] = gpool_doubles;
+      gpool_doubles += static_cast<long long>(grids[g]) * per_cta * Lmax * team;
+    }
+  }
+  void* d_gpool = nullptr;
+  if (gpool_doubles > 0 &&
+      (st = ex.buffer(kGpool, static_cast<size_t>(gpool_doubles) * sizeof(double), &d_gpool)) != WLG_OK)
+    return st;
+  if (ex.ev != nullptr) cudaEventRecord(ex.ev[2], ex.stream);
+  for (size_t g = 0; g < launches.size(); ++g) {
+    const auto [variant, team, bytes, per_cta, first, count, Lmax] = launches[g];
+    const int grid = grids[g];
+    double* gp = variant == 3 ? static_cast<double*>(d_gpool) + gpool_off[g] : nullptr;
     st = wlg::launch_main_batch(variant, static_cast<const MainDesc*>(d_md), static_cast<const int*>(d_order) + first,
-                                count, team, bytes, per_cta, grid, static_cast<int*>(d_next) + g,
+                                count, team, bytes, per_cta, grid, static_cast<int*>(d_next) + g, gp,
+                                static_cast<long long>(Lmax) * team,
                                 static_cast<const uint32_t*>(d_Jw), static_cast<const uint32_t*>(d_latw),
                                 static_cast<const int*>(d_win), static_cast<const uint32_t*>(d_mask),
                                 static_cast<double*>(d_out), static_cast<MainResult*>(d_res), nullptr, ex.stream);
     if (st != WLG_OK) return fail(ex, st, "main-run launch failed");
     ++ex.launches;
+    ex.main_forms |= 1 << variant;
   }
   if (ex.ev != nullptr) cudaEventRecord(ex.ev[3], ex.stream);
   download(ex, d_res, mres);
@@ -647,6 +701,7 @@ void keep_stats(wlg_context* ctx, const Exec& ex)
   ctx->h2d = ex.h2d;
   ctx->d2h = ex.d2h;
   ctx->launches = ex.launches;
+  ctx->main_forms = ex.main_forms;
   if (!ex.err.empty()) ctx->err = ex.err;
 }
 
@@ -818,6 +873,7 @@ wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)
   out->h2d_bytes = ctx->h2d;
   out->d2h_bytes = ctx->d2h;
   out->kernel_launches = ctx->launches;
+  out->main_forms = ctx->main_forms;
   return WLG_OK;
 }
 

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def oracle_run(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc,
-               xmode, gpar):
+               xmode, gpar, max_outer=0):
     N = X * Y
     seen = np.zeros(R * (4 * N + 1), np.uint8)
     J = np.zeros(R * 2 * N, np.int8)
@@ -33,8 +33,9 @@ def oracle_run(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, ov
     ci = np.zeros(R, np.int32)
     outer = C.c_longlong(0)
     flips = C.c_longlong(0)
-    args = (X, Y, boundary, R, I, W, C.c_float(overlap), alpha, beta, n_iter, xc, xmode, gpar, seed, 0, O.ptr(seen),
-            O.ptr(J), O.ptr(flat), O.ptr(flag), O.ptr(en), pre_i, O.ptr(start), O.ptr(end), O.ptr(off_hist))
+    args = (X, Y, boundary, R, I, W, C.c_float(overlap), alpha, beta, n_iter, xc, xmode, gpar, seed,
+            max_outer, O.ptr(seen), O.ptr(J), O.ptr(flat), O.ptr(flag), O.ptr(en), pre_i, O.ptr(start), O.ptr(end),
+            O.ptr(off_hist))
     st = L.orc_mainrun(*args, None, C.byref(n_log), O.ptr(ci), C.byref(outer), C.byref(flips))
     logG = np.zeros(max(n_log.value, 1), np.float64)
     st = L.orc_mainrun(*args, O.ptr(logG), C.byref(n_log), O.ptr(ci), C.byref(outer), C.byref(flips))
@@ -94,6 +95,64 @@ def test_engine_full_run_bit_exact(cuda, cfg):
         assert np.array_equal(G, Go[:nout.value])
         lse = np.logaddexp.reduce(G)
         assert abs(lse - X * Y * np.log(2)) < 1e-9
+
+
+# Problems whose per-team state (FP64 + float log g, histogram, lattices) is
+# above 227 KB of shared memory: the main run keeps FP64 log g in a global
+# pool (form 3).  Capped at three outer iterations; the cap ends both sides at
+# the same point.
+BIG = [
+    # 16x16, one window of 96 walkers: 192 bins x 96 walkers x 16 B = 295 KB
+    (16, 16, 0, 0.04, "i", 12345, 1, 128, 32, 2000, 1, 96, 0.25, 0.8, 1e-3, 1000, 20, 1, 0),
+    # 20x20, two windows of 48 walkers exchanging every iteration: 212 bins x 96 walkers x 16 B = 326 KB
+    (20, 20, 0, 0.04, "v", 12345, 1, 128, 32, 2000, 2, 48, 0.25, 0.8, 1e-3, 500, 1, 1, 0),
+]
+
+
+def big_problems(cfg, R=None, max_outer=3):
+    import qec_pf_wang_landau_gb300 as wlg
+    (X, Y, boundary, prob, cls, seed, R0, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc, xmode,
+     gpar) = cfg
+    return [wlg.problem(X, Y, boundary=boundary, prob=prob, error_class=cls, seed=seed, sample=k,
+                        pre_walkers=pre_w, pre_intervals=pre_i, pre_iterations=pre_n, intervals=I,
+                        walkers_per_interval=W, overlap=overlap, alpha=alpha, beta=beta, iterations=n_iter,
+                        exchange_every=xc, exchange_mode=xmode, global_parity=gpar, max_outer=max_outer)
+            for k in range(R0 if R is None else R)]
+
+
+@pytest.mark.parametrize("cfg", BIG, ids=[f"{c[0]}x{c[1]}I{c[10]}W{c[11]}" for c in BIG])
+def test_engine_global_log_g_form_bit_exact(cuda, cfg):
+    import qec_pf_wang_landau_gb300 as wlg
+    I = cfg[10]
+    ref = oracle_run(*cfg, max_outer=3)
+    assert ref["status"] == 3 and ref["outer"] == 3
+    ctx = wlg.Context(0)
+    out = ctx.solve_raw(big_problems(cfg))
+    assert ctx.stats()["main_forms"] == 1 << 3
+    (res, s, e, wins), = out
+    assert res.status == wlg.WLG_ERR_TIMEOUT and res.outer_iterations == 3
+    assert res.flips == ref["flips"]
+    assert np.array_equal(s, ref["start"][:I]) and np.array_equal(e, ref["end"][:I])
+    for b in range(I):
+        o = ref["off_hist"][b * cfg[11]]
+        want = ref["logG"][o:o + (e[b] - s[b] + 1)]
+        assert np.array_equal(wins[b], want), f"window {b}: max |d| {np.abs(wins[b] - want).max()}"
+
+
+def test_engine_mixed_forms_batch_equals_separate_runs(cuda):
+    """A batch holding shared-memory-form and global-pool-form problems (two
+    persistent launches, one global pool) gives each problem its result alone."""
+    import qec_pf_wang_landau_gb300 as wlg
+    small = wlg.problem(6, 6, prob=0.04, error_class="h", seed=12345, sample=3, max_outer=3)
+    batch = [big_problems(BIG[1])[0], small, big_problems(BIG[0])[0]]
+    ctx = wlg.Context(0)
+    together = ctx.solve_raw(batch)
+    assert ctx.stats()["main_forms"] & (1 << 3) and ctx.stats()["main_forms"] != 1 << 3
+    for p, (r, s, e, wins) in zip(batch, together):
+        (r1, s1, e1, wins1), = ctx.solve_raw([p])
+        assert r.status == r1.status and r.flips == r1.flips and r.outer_iterations == r1.outer_iterations
+        assert np.array_equal(s, s1) and np.array_equal(e, e1)
+        assert all(np.array_equal(a, b) for a, b in zip(wins, wins1))
 
 
 def test_engine_heterogeneous_batch_equals_separate_runs(cuda):
