@@ -317,13 +317,36 @@ def run_reference(args):
     }
 
 
+def profile_case(name: str):
+    """Small fixed cases for ncu captures (not bench numbers): `main6x6` = 152
+    problems of the workload (samples 0-37 x ivhc, one per SM) capped at 20
+    outer iterations, solved twice (capture the second main-run launch)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    wlg.build()
+    if name != "main6x6":
+        raise SystemExit(f"unknown profile case {name}")
+    probs = problems(0)[:152]
+    for p in probs:
+        p.max_outer = 20
+    ctx = wlg.Context(0)
+    for _ in range(2):
+        out = ctx.solve_raw(probs)
+    st = ctx.stats()
+    steps = sum(r.flips for r, _, _, _ in out) / 30
+    print(json.dumps({"case": name, "main_ms": st["main_ms"], "walker_steps_per_warp": steps / len(probs)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--profile-case", default=None, help="run a small fixed case for a profiler and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)

@@ -34,6 +34,7 @@
 #include "wlg_internal.h"
 #include "wlg_lattice.cuh"
 #include "wlg_rng.cuh"
+#include "wlg_shadow.cuh"
 
 namespace wlg {
 namespace {
@@ -171,13 +172,19 @@ struct Team {
 // integer; there the reference's own float/double expression decides.  No
 // int<->float conversion on the common path (they share GB300's slow FP64
 // pipe).
-__device__ __forceinline__ int pick_site(uint32_t x, const MainDesc& d)
+// The reference's site pick in FP64 (wl.cu:60-66), for draws whose product
+// with N lies next to a cell boundary.  Out of line: inlined, its FP64
+// multiply and conversions would be scheduled into every step.
+__device__ __noinline__ int site_exact(uint32_t x, double scale)
 {
-  const uint32_t n = static_cast<uint32_t>(d.N);
-  const uint32_t lo = x * n;
-  int s = static_cast<int>(__umulhi(x, n));
-  if (lo < d.site_thr || lo > ~d.site_thr) s = static_cast<int>(trunc(static_cast<double>(unit_float(x)) * d.site_scale));
-  return s;
+  return static_cast<int>(trunc(static_cast<double>(unit_float(x)) * scale));
+}
+
+// The reference's acceptance u < min(1, exp(g - g_new)) (wl.cu:1113-1116)
+// in FP64, out of line (rare path; see site_exact).
+__device__ __noinline__ bool accept_exact(uint32_t x2, double g, const double* g_new)
+{
+  return static_cast<double>(unit_float(x2)) < fmin(1.0, exp(g - *g_new));
 }
 
 struct Lat {
@@ -385,9 +392,17 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       status = WLG_ERR_TIMEOUT;
       break;
     }
-    // ---- WL sweep (wl.cu:1077-1175).  One uniform, branch-free step body:
-    // the acceptance draw is peeked and used only for in-window proposals,
-    // the Philox block after next is computed speculatively every step.
+    // ---- WL sweep (wl.cu:1077-1175).  The step body has no divergent
+    // branch: every state update is predicated on `commit`.  The two FP64
+    // decisions of the reference that FP32 cannot always settle (a site pick
+    // next to a cell boundary, an acceptance inside the FP32 error band) are
+    // made for the few lanes that need them in a warp-uniform block at the
+    // end of the body, after which those lanes replay the same step (same
+    // draws) with the exact answer.  Each lane counts its own steps; the warp
+    // loops until all of its live lanes are done.  The acceptance draw is
+    // peeked and consumed only for in-window proposals, and the Philox block
+    // after next is computed speculatively every step.
+    const unsigned wmask = __ballot_sync(0xFFFFFFFFu, live);
     if (live) {
       const bool frozen = cond[b] != 0;
       const double lnf = log(fwin[b]);
@@ -399,25 +414,41 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       // relative shadow keeps the FP32 error bound (and the FP64 fallback
       // rate) small
       const double gbase = g_cur;
+      const Bits gbase_bits = split_bits(gbase);
       for (int c = 0; c < d.L; ++c) Gf[c * P + t] = static_cast<float>(G[c * P + t] - gbase);
       // one rounding of a double of size |g| <= |gbase| + (small shadow terms)
       const float ulp_g = static_cast<float>((fabs(gbase) + 1.0) * 0x1p-51);
       float gfb = 0.0f;               // float of g_cur - gbase at the last change of bin
       uint32_t h_cur = H[c_cur * P + t];
       float kf = 0.0f;                // ln f increments since then (exact below 2^24)
+      // ln f owed to g_cur by the previous step (wl.cu:1124), added one step
+      // late so the FP64 addition overlaps the next step's decision instead
+      // of waiting on a shared-memory load; same additions, same order
+      double owed = 0.0;
       uint64_t pos = rng.pos;
       uint64_t blk = pos >> 2;
       uint4 A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), rng.s0, rng.s1, rng.k0, rng.k1);
       uint4 B = philox10(static_cast<uint32_t>(blk + 1), static_cast<uint32_t>((blk + 1) >> 32), rng.s0, rng.s1,
                          rng.k0, rng.k1);
-      for (int it = 0; it < d.n_iter; ++it) {
+      const uint32_t nN = static_cast<uint32_t>(d.N);
+      int it = 0;
+      bool stopped = false;
+      int ovr_site = -1;  // exact site of the step being replayed
+      int ovr_acc = -1;   // exact acceptance of the step being replayed
+      for (;;) {
+        const bool act = it < d.n_iter && !stopped;
+        if (!__any_sync(wmask, act)) break;
         const uint64_t nx = blk + 2;
         const uint4 Cn = philox10(static_cast<uint32_t>(nx), static_cast<uint32_t>(nx >> 32), rng.s0, rng.s1, rng.k0,
                                   rng.k1);
         const int q = static_cast<int>(pos - (blk << 2));
         const uint32_t x1 = pick_word(A, B, q);
         const uint32_t x2 = pick_word(A, B, q + 1);
-        const int site = pick_site(x1, d);
+        // site trunc(u (N - 1 + 0.999999)) (wl.cu:60-66) as floor(x N / 2^32)
+        // unless x N lies within site_thr of a multiple of 2^32
+        const uint32_t lo_s = x1 * nN;
+        const bool need_site = act && ovr_site < 0 && (lo_s < d.site_thr || lo_s > ~d.site_thr);
+        const int site = ovr_site >= 0 ? ovr_site : static_cast<int>(__umulhi(x1, nN));
         int En;
         if constexpr (kTable) {
           const ulonglong2 nt = nbt[site];
@@ -435,9 +466,10 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const int c_new = min(max((En - bb) >> d.lg, 0), Lm1);
         const bool same = c_new == c_cur;
         const float gfn = Gf[c_new * P + t];
+        const uint32_t h_new = H[c_new * P + t];
+        const double g_new = kGlobalG ? 0.0 : G[c_new * P + t];
         // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) from FP32 values
-        // with a proven error bound eps on the exponent; the reference's FP64
-        // expression decides whenever the bound does not.  For a
+        // with a proven error bound eps on the exponent.  For a
         // non-negative exponent the test is u < 1, i.e. x2 < 2^32 - 128
         // exactly; otherwise u is approximated without a conversion as
         // (x2 >> 9) 2^-23 (error < 2^-22, margin 2^-21).
@@ -452,47 +484,56 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const float r = 1.1f * (eps + (2.0f + 1.2f * fabsf(df)) * 0x1p-23f) + 0x1p-22f;
         const float t_lo = e * (1.0f - r), t_hi = e * (1.0f + r);
         const float ua = __int_as_float(0x3F800000u | (x2 >> 9)) - 1.0f;
-        bool acc = nonneg ? (x2 < 0xFFFFFF80u) : (ua + 0x1p-21f < t_lo);
+        const bool fast_acc = nonneg ? (x2 < 0xFFFFFF80u) : (ua + 0x1p-21f < t_lo);
         const bool known = nonneg || (df + eps < 0.0f && (ua + 0x1p-21f < t_lo || ua - 0x1p-21f >= t_hi));
-        if (inside && !known) {
-          const double gn = G[c_new * P + t];
-          acc = static_cast<double>(unit_float(x2)) < fmin(1.0, exp(g_cur - gn));
-        }
-        if (bad) {  // wl.cu:1091-1104: a new energy stops the problem
-          ++pos;
+        const bool need_acc = act && !need_site && !bad && inside && ovr_acc < 0 && !known;
+        g_cur += owed;  // g >= +0, so adding +0 (frozen, first step) is exact
+        owed = 0.0;
+        const bool stop_now = act && !need_site && bad;  // wl.cu:1091-1104: a new energy stops the problem
+        if (stop_now) {
           misc[1] = 1;
           misc[2] = En;
-          break;
         }
-        acc = acc && inside;
+        const bool commit = act && !need_site && !need_acc && !bad;
+        const bool acc = commit && inside && (ovr_acc >= 0 ? ovr_acc != 0 : fast_acc);
         flip_spin<kReg>(lt, site, acc);
         E = acc ? En : E;
-        const bool change = acc && !same;
-        if (!frozen) {
-          if (change) {
-            G[c_cur * P + t] = g_cur;
-            Gf[c_cur * P + t] = static_cast<float>(g_cur - gbase);
-            H[c_cur * P + t] = h_cur;
-            g_cur = G[c_new * P + t];
-            h_cur = H[c_new * P + t];
-            gfb = gfn;
-            kf = 0.0f;
-            c_cur = c_new;
-          }
-          g_cur += lnf;
-          h_cur += 1u;
-          kf += 1.0f;
-        } else if (change) {
-          g_cur = G[c_new * P + t];
-          gfb = gfn;
-          c_cur = c_new;
+        // leaving c_cur: write back its log g, shadow and visit count
+        const bool chg = acc && !same;
+        const float sh = shadow_of(g_cur, gbase_bits);
+        if (chg && !frozen) {
+          G[c_cur * P + t] = g_cur;
+          Gf[c_cur * P + t] = sh;
+          H[c_cur * P + t] = h_cur;
         }
-        pos += inside ? 2 : 1;
+        if constexpr (kGlobalG) {
+          if (chg) g_cur = G[c_new * P + t];
+        } else {
+          g_cur = chg ? g_new : g_cur;
+        }
+        h_cur = chg ? h_new : h_cur;
+        gfb = chg ? gfn : gfb;
+        kf = chg ? 0.0f : kf;
+        c_cur = chg ? c_new : c_cur;
+        const bool upd = commit && !frozen;
+        owed = upd ? lnf : 0.0;
+        h_cur += upd ? 1u : 0u;
+        kf += upd ? 1.0f : 0.0f;
+        pos += commit ? (inside ? 2 : 1) : (stop_now ? 1 : 0);
+        it += commit ? 1 : 0;
+        stopped = stopped || stop_now;
+        ovr_site = commit || stop_now ? -1 : ovr_site;
+        ovr_acc = commit || stop_now ? -1 : ovr_acc;
         const bool adv = (pos >> 2) != blk;
         A = adv ? B : A;
         B = adv ? Cn : B;
         blk = adv ? blk + 1 : blk;
+        if (__any_sync(wmask, need_site || need_acc)) {  // rare
+          if (need_site) ovr_site = site_exact(x1, d.site_scale);
+          if (need_acc) ovr_acc = accept_exact(x2, g_cur, G + c_new * P + t) ? 1 : 0;
+        }
       }
+      g_cur += owed;
       if (!frozen) {
         G[c_cur * P + t] = g_cur;
         H[c_cur * P + t] = h_cur;

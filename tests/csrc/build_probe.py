@@ -8,7 +8,8 @@ LIB = os.path.join(HERE, "libprobe.so")
 
 def build() -> str:
     src = os.path.join(HERE, "curand_probe.cu")
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    dep = os.path.join(HERE, "..", "..", "qec_pf_wang_landau_gb300", "csrc", "wlg_shadow.cuh")
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(dep)):
         return LIB
     subprocess.run(["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC",
                     "-shared", "-o", LIB + ".tmp", src], check=True)

@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <curand_kernel.h>
 
+#include "../../qec_pf_wang_landau_gb300/csrc/wlg_shadow.cuh"
+
 namespace {
 
 __global__ void k_curand(const unsigned long long* seeds, const unsigned long long* subseqs,
@@ -40,9 +42,22 @@ __global__ void k_fast_exp(const float* x, float* y, int n)
   if (q < n) y[q] = __expf(x[q]);
 }
 
+__global__ void k_shadow(const double* g, const double* base, float* out, int n)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) out[q] = wlg::shadow_of(g[q], wlg::split_bits(base[q]));
+}
+
 }  // namespace
 
 extern "C" {
+
+// The engine's integer-formed log g shadows (wlg_shadow.cuh) for n pairs.
+int probe_shadow(const double* d_g, const double* d_base, float* d_out, int n)
+{
+  k_shadow<<<(n + 127) / 128, 128>>>(d_g, d_base, d_out, n);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
 
 int probe_fast_exp(const float* d_x, float* d_y, int n)
 {
