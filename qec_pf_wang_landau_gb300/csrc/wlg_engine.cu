@@ -484,8 +484,14 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const float r = 1.1f * (eps + (2.0f + 1.2f * fabsf(df)) * 0x1p-23f) + 0x1p-22f;
         const float t_lo = e * (1.0f - r), t_hi = e * (1.0f + r);
         const float ua = __int_as_float(0x3F800000u | (x2 >> 9)) - 1.0f;
+        // Known without FP64: a non-negative exponent (u < 1); u below the
+        // lower bound t_lo of min(1, exp(.)) (accept); for a surely negative
+        // exponent u at or above the upper bound t_hi (reject); when the
+        // exponent straddles 0, min(1, exp(.)) lies in [t_lo, 1], so u = 1
+        // (reject) is known too and only u in [t_lo, 1) is not.
         const bool fast_acc = nonneg ? (x2 < 0xFFFFFF80u) : (ua + 0x1p-21f < t_lo);
-        const bool known = nonneg || (df + eps < 0.0f && (ua + 0x1p-21f < t_lo || ua - 0x1p-21f >= t_hi));
+        const bool known = nonneg || ua + 0x1p-21f < t_lo ||
+                           (df + eps < 0.0f ? ua - 0x1p-21f >= t_hi : x2 >= 0xFFFFFF80u);
         const bool need_acc = act && !need_site && !bad && inside && ovr_acc < 0 && !known;
         g_cur += owed;  // g >= +0, so adding +0 (frozen, first step) is exact
         owed = 0.0;
