@@ -19,10 +19,11 @@
 //     over energies the lattice can reach (every 2nd or 4th value);
 //   * the current bin's log g and count cached in registers, written back
 //     only when the walker changes energy.
-// Acceptance min(1, exp(dlogg)) is decided with FP32 values and a proven
-// error bound on the exponent (float shadows of log g, __expf); inside the
-// band, and for the site pick near a bin edge, the exact FP64 expression of
-// the reference decides, so every decision equals the reference's.
+// Acceptance u < min(1, exp(dlogg)) is decided as log u < dlogg with FP32
+// values and proven error bounds (float shadows of log g, __logf of the
+// uniform); inside the band, and for the site pick near a bin edge, the exact
+// FP64 expression of the reference decides, so every decision equals the
+// reference's.
 
 #include <cuda_runtime.h>
 
@@ -33,6 +34,7 @@
 #include "wlg_engine.h"
 #include "wlg_internal.h"
 #include "wlg_lattice.cuh"
+#include "wlg_accept.cuh"
 #include "wlg_rng.cuh"
 #include "wlg_shadow.cuh"
 
@@ -169,12 +171,10 @@ struct Team {
 // f = x / 2^32 the reference's product lies within N*2^-23 + 1e-6 of f*N, so
 // floor(f*N) = umulhi(x, N) is exact unless the fraction x*N mod 2^32 lies
 // within site_thr (= 2^32 (N 2^-21 + 2^-18), >= 4x that bound) of an
-// integer; there the reference's own float/double expression decides.  No
-// int<->float conversion on the common path (they share GB300's slow FP64
-// pipe).
-// The reference's site pick in FP64 (wl.cu:60-66), for draws whose product
-// with N lies next to a cell boundary.  Out of line: inlined, its FP64
-// multiply and conversions would be scheduled into every step.
+// integer; there the reference's own float/double expression below decides.
+// No int<->float conversion on the common path (they share GB300's slow
+// FP64 pipe).  Out of line: inlined, its FP64 multiply and conversions would
+// be scheduled into every step.
 __device__ __noinline__ int site_exact(uint32_t x, double scale)
 {
   return static_cast<int>(trunc(static_cast<double>(unit_float(x)) * scale));
@@ -444,6 +444,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const int q = static_cast<int>(pos - (blk << 2));
         const uint32_t x1 = pick_word(A, B, q);
         const uint32_t x2 = pick_word(A, B, q + 1);
+        const float lu = log_uniform(x2);  // depends on the draw only: off the serial path
         // site trunc(u (N - 1 + 0.999999)) (wl.cu:60-66) as floor(x N / 2^32)
         // unless x N lies within site_thr of a multiple of 2^32
         const uint32_t lo_s = x1 * nN;
@@ -468,30 +469,18 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const float gfn = Gf[c_new * P + t];
         const uint32_t h_new = H[c_new * P + t];
         const double g_new = kGlobalG ? 0.0 : G[c_new * P + t];
-        // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) from FP32 values
-        // with a proven error bound eps on the exponent.  For a
-        // non-negative exponent the test is u < 1, i.e. x2 < 2^32 - 128
-        // exactly; otherwise u is approximated without a conversion as
-        // (x2 >> 9) 2^-23 (error < 2^-22, margin 2^-21).
+        // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) decided from FP32
+        // values with a proven error bound eps on the exponent; the
+        // reference's FP64 expression decides whenever the bound does not.
         const float kl = kf * lnf_f;
         const float df = (gfb - gfn) + kl;
         // |df - (g_cur - g_new)|: float roundings of the shadows and of df
         // (2^-22 = 4x their 2^-24), plus the k sequential double additions in
         // g_cur and the double differences, each <= one rounding at |g|
         const float eps = 0x1p-22f * (fabsf(gfb) + fabsf(gfn) + kl + fabsf(df)) + (kf + 4.0f) * ulp_g;
-        const bool nonneg = same || df - eps >= 0.0f;
-        const float e = __expf(df);
-        const float r = 1.1f * (eps + (2.0f + 1.2f * fabsf(df)) * 0x1p-23f) + 0x1p-22f;
-        const float t_lo = e * (1.0f - r), t_hi = e * (1.0f + r);
-        const float ua = __int_as_float(0x3F800000u | (x2 >> 9)) - 1.0f;
-        // Known without FP64: a non-negative exponent (u < 1); u below the
-        // lower bound t_lo of min(1, exp(.)) (accept); for a surely negative
-        // exponent u at or above the upper bound t_hi (reject); when the
-        // exponent straddles 0, min(1, exp(.)) lies in [t_lo, 1], so u = 1
-        // (reject) is known too and only u in [t_lo, 1) is not.
-        const bool fast_acc = nonneg ? (x2 < 0xFFFFFF80u) : (ua + 0x1p-21f < t_lo);
-        const bool known = nonneg || ua + 0x1p-21f < t_lo ||
-                           (df + eps < 0.0f ? ua - 0x1p-21f >= t_hi : x2 >= 0xFFFFFF80u);
+        const Decision dec = decide(x2, lu, df, eps, same);
+        const bool fast_acc = dec.acc;
+        const bool known = dec.known;
         const bool need_acc = act && !need_site && !bad && inside && ovr_acc < 0 && !known;
         g_cur += owed;  // g >= +0, so adding +0 (frozen, first step) is exact
         owed = 0.0;

@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <curand_kernel.h>
 
+#include "../../qec_pf_wang_landau_gb300/csrc/wlg_accept.cuh"
 #include "../../qec_pf_wang_landau_gb300/csrc/wlg_shadow.cuh"
 
 namespace {
@@ -48,9 +49,47 @@ __global__ void k_shadow(const double* g, const double* base, float* out, int n)
   if (q < n) out[q] = wlg::shadow_of(g[q], wlg::split_bits(base[q]));
 }
 
+// max |__logf(x) - log(x)| over the floats with bit patterns [lo, hi]
+__global__ void k_logf_maxerr(unsigned lo, unsigned hi, unsigned* max_bits)
+{
+  float worst = 0.0f;
+  for (unsigned long long b = lo + blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; b <= hi;
+       b += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    const float x = __uint_as_float(static_cast<unsigned>(b));
+    const double err = fabs(static_cast<double>(__logf(x)) - log(static_cast<double>(x)));
+    worst = fmaxf(worst, __double2float_ru(err));
+  }
+  atomicMax(max_bits, __float_as_uint(worst));
+}
+
+// decide() against the exact rule u < min(1, exp(d)) for n draws with
+// estimates df = d + noise, |noise| <= eps
+__global__ void k_decide(const unsigned* x, const double* d, const float* df, const float* eps, int n, int* out)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const wlg::Decision r = wlg::decide(x[q], wlg::log_uniform(x[q]), df[q], eps[q], false);
+  const bool exact = static_cast<double>(wlg::unit_float(x[q])) < fmin(1.0, exp(d[q]));
+  out[q] = r.known ? (r.acc == exact ? 1 : -1) : 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+float probe_log_bound() { return wlg::kLogAbsErr; }
+
+int probe_logf_maxerr(unsigned lo, unsigned hi, unsigned* d_max_bits)
+{
+  k_logf_maxerr<<<152 * 8, 256>>>(lo, hi, d_max_bits);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
+int probe_decide(const unsigned* d_x, const double* d_d, const float* d_df, const float* d_eps, int n, int* d_out)
+{
+  k_decide<<<(n + 127) / 128, 128>>>(d_x, d_d, d_df, d_eps, n, d_out);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
 
 // The engine's integer-formed log g shadows (wlg_shadow.cuh) for n pairs.
 int probe_shadow(const double* d_g, const double* d_base, float* d_out, int n)

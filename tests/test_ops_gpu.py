@@ -396,6 +396,48 @@ def test_integer_shadow_within_one_float_rounding(cuda, probe):
         assert err <= bound * abs(exact), (g[q], base[q], out[q])
 
 
+def test_fast_log_error_within_engine_bound(cuda, probe):
+    """The sweep decides log u < d with u's __logf; its error bound holds for
+    every float u in [2^-33, 1] (exhaustive, against FP64 log)."""
+    torch = cuda
+    probe.probe_log_bound.restype = C.c_float
+    bound = probe.probe_log_bound()
+    mx = torch.zeros(1, dtype=torch.int32, device="cuda")
+    probe.probe_logf_maxerr.argtypes = [C.c_uint, C.c_uint, C.c_void_p]
+    lo = int(np.float32(2.0 ** -33).view(np.uint32))
+    hi = int(np.float32(1.0).view(np.uint32))
+    assert probe.probe_logf_maxerr(lo, hi, _dptr(mx)) == 0
+    worst = float(mx.cpu().numpy().view(np.float32)[0])
+    assert 0.0 < worst <= bound, (worst, bound)
+
+
+def test_fast_decision_never_contradicts_exact_rule(cuda, probe):
+    """decide(): whenever it reports the answer as known it equals the
+    reference's u < min(1, exp(d)), for estimates df within eps of d, most of
+    all next to the boundary log u = d."""
+    torch = cuda
+    rng = np.random.default_rng(11)
+    n = 2_000_000
+    x = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    x[:1000] = 0xFFFFFFFF - np.arange(1000, dtype=np.uint32)  # u = 1
+    u = ((x.astype(np.float64) + 0.5) * 2.0 ** -32).astype(np.float32).astype(np.float64)
+    d = rng.uniform(-12.0, 1.0, n)
+    near = rng.random(n) < 0.5
+    d[near] = np.log(u[near]) + rng.choice([-1.0, 1.0], near.sum()) * 10.0 ** rng.uniform(-9, -3, near.sum())
+    eps = (10.0 ** rng.uniform(-9, -4, n)).astype(np.float32)
+    noise = rng.uniform(-0.5, 0.5, n) * eps
+    df = (d + noise).astype(np.float32)
+    eps = (eps.astype(np.float64) + np.abs(df.astype(np.float64) - (d + noise))).astype(np.float32) * np.float32(1.0001)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    tx, td, tdf, te = dev(x.view(np.int32)), dev(d), dev(df), dev(eps)
+    out = torch.zeros(n, dtype=torch.int32, device="cuda")
+    probe.probe_decide.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
+    assert probe.probe_decide(_dptr(tx), _dptr(td), _dptr(tdf), _dptr(te), n, _dptr(out)) == 0
+    o = out.cpu().numpy()
+    assert (o >= 0).all(), int((o < 0).sum())
+    assert (o[~near] == 0).mean() < 1e-3   # away from the boundary almost everything is settled in FP32
+
+
 def test_device_exp_of_nonnegative_is_at_least_one(cuda, probe):
     """min(1, exp(d)) == 1 for every d >= 0 (the acceptance shortcut for d >= 0)."""
     torch = cuda
