@@ -414,7 +414,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       // relative shadow keeps the FP32 error bound (and the FP64 fallback
       // rate) small
       const double gbase = g_cur;
-      const Bits gbase_bits = split_bits(gbase);
+      const Split gbase_split = split_float(gbase);
       for (int c = 0; c < d.L; ++c) Gf[c * P + t] = static_cast<float>(G[c * P + t] - gbase);
       // one rounding of a double of size |g| <= |gbase| + (small shadow terms)
       const float ulp_g = static_cast<float>((fabs(gbase) + 1.0) * 0x1p-51);
@@ -425,11 +425,20 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       // late so the FP64 addition overlaps the next step's decision instead
       // of waiting on a shared-memory load; same additions, same order
       double owed = 0.0;
+      // Draws: A and B hold the outputs of counters blk and blk + 1; C is
+      // Philox of counter blk + 2, advanced five rounds per step (phase
+      // 0, 1: rounds done 0, 5; 2: complete).  A step consumes at most two
+      // draws, so after C is restarted two steps pass before B runs out
+      // and C, complete by then, replaces it.
       uint64_t pos = rng.pos;
       uint64_t blk = pos >> 2;
       uint4 A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), rng.s0, rng.s1, rng.k0, rng.k1);
       uint4 B = philox10(static_cast<uint32_t>(blk + 1), static_cast<uint32_t>((blk + 1) >> 32), rng.s0, rng.s1,
                          rng.k0, rng.k1);
+      uint4 Cb = philox10(static_cast<uint32_t>(blk + 2), static_cast<uint32_t>((blk + 2) >> 32), rng.s0, rng.s1,
+                          rng.k0, rng.k1);
+      int phase = 2;
+      const uint32_t k5a = rng.k0 + 5u * kPhiloxWeylA, k5b = rng.k1 + 5u * kPhiloxWeylB;  // key of round 5
       const uint32_t nN = static_cast<uint32_t>(d.N);
       int it = 0;
       bool stopped = false;
@@ -438,9 +447,11 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       for (;;) {
         const bool act = it < d.n_iter && !stopped;
         if (!__any_sync(wmask, act)) break;
-        const uint64_t nx = blk + 2;
-        const uint4 Cn = philox10(static_cast<uint32_t>(nx), static_cast<uint32_t>(nx >> 32), rng.s0, rng.s1, rng.k0,
-                                  rng.k1);
+        {
+          const uint4 half = philox_rounds<5>(Cb, phase == 0 ? rng.k0 : k5a, phase == 0 ? rng.k1 : k5b);
+          Cb = phase < 2 ? half : Cb;
+          phase = min(phase + 1, 2);
+        }
         const int q = static_cast<int>(pos - (blk << 2));
         const uint32_t x1 = pick_word(A, B, q);
         const uint32_t x2 = pick_word(A, B, q + 1);
@@ -474,10 +485,12 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         // reference's FP64 expression decides whenever the bound does not.
         const float kl = kf * lnf_f;
         const float df = (gfb - gfn) + kl;
-        // |df - (g_cur - g_new)|: float roundings of the shadows and of df
-        // (2^-22 = 4x their 2^-24), plus the k sequential double additions in
-        // g_cur and the double differences, each <= one rounding at |g|
-        const float eps = 0x1p-22f * (fabsf(gfb) + fabsf(gfn) + kl + fabsf(df)) + (kf + 4.0f) * ulp_g;
+        // |df - (g_cur - g_new)|: the shadows' relative errors (<= 2^-23)
+        // and the float roundings of kl and df (2^-22 = 2x and 4x them); the k
+        // sequential double additions in g_cur and the double differences,
+        // each <= one rounding at |g| (k + 4 ulp_g); the shadows' absolute
+        // error 2^-44 (g + gbase) each (<= 512 ulp_g for both)
+        const float eps = 0x1p-22f * (fabsf(gfb) + fabsf(gfn) + kl + fabsf(df)) + (kf + 516.0f) * ulp_g;
         const Decision dec = decide(x2, lu, df, eps, same);
         const bool fast_acc = dec.acc;
         const bool known = dec.known;
@@ -495,7 +508,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         E = acc ? En : E;
         // leaving c_cur: write back its log g, shadow and visit count
         const bool chg = acc && !same;
-        const float sh = shadow_of(g_cur, gbase_bits);
+        const float sh = shadow_split(g_cur, gbase_split);
         if (chg && !frozen) {
           G[c_cur * P + t] = g_cur;
           Gf[c_cur * P + t] = sh;
@@ -521,8 +534,11 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         ovr_acc = commit || stop_now ? -1 : ovr_acc;
         const bool adv = (pos >> 2) != blk;
         A = adv ? B : A;
-        B = adv ? Cn : B;
+        B = adv ? Cb : B;
         blk = adv ? blk + 1 : blk;
+        const uint64_t nc = blk + 2;  // restart C on the counter after the new B
+        Cb = adv ? make_uint4(static_cast<uint32_t>(nc), static_cast<uint32_t>(nc >> 32), rng.s0, rng.s1) : Cb;
+        phase = adv ? 0 : phase;
         if (__any_sync(wmask, need_site || need_acc)) {  // rare
           if (need_site) ovr_site = site_exact(x1, d.site_scale);
           if (need_acc) ovr_acc = accept_exact(x2, g_cur, G + c_new * P + t) ? 1 : 0;

@@ -26,23 +26,31 @@ constexpr uint32_t kPhiloxMulB = 0xCD9E8D57u;
 constexpr uint32_t kPhiloxWeylA = 0x9E3779B9u;
 constexpr uint32_t kPhiloxWeylB = 0xBB67AE85u;
 
-__device__ __forceinline__ uint4 philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
-                                          uint32_t k1)
+// kRounds Philox4x32 rounds applied to the state c, the first of them under
+// the key (k0, k1); the key advances by the Weyl constants every round.
+template <int kRounds>
+__device__ __forceinline__ uint4 philox_rounds(uint4 c, uint32_t k0, uint32_t k1)
 {
 #pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint64_t pa = static_cast<uint64_t>(kPhiloxMulA) * c0;
-    const uint64_t pb = static_cast<uint64_t>(kPhiloxMulB) * c2;
-    const uint32_t n0 = static_cast<uint32_t>(pb >> 32) ^ c1 ^ k0;
-    const uint32_t n2 = static_cast<uint32_t>(pa >> 32) ^ c3 ^ k1;
-    c1 = static_cast<uint32_t>(pb);
-    c3 = static_cast<uint32_t>(pa);
-    c0 = n0;
-    c2 = n2;
+  for (int r = 0; r < kRounds; ++r) {
+    const uint64_t pa = static_cast<uint64_t>(kPhiloxMulA) * c.x;
+    const uint64_t pb = static_cast<uint64_t>(kPhiloxMulB) * c.z;
+    const uint32_t n0 = static_cast<uint32_t>(pb >> 32) ^ c.y ^ k0;
+    const uint32_t n2 = static_cast<uint32_t>(pa >> 32) ^ c.w ^ k1;
+    c.y = static_cast<uint32_t>(pb);
+    c.w = static_cast<uint32_t>(pa);
+    c.x = n0;
+    c.z = n2;
     k0 += kPhiloxWeylA;
     k1 += kPhiloxWeylB;
   }
-  return make_uint4(c0, c1, c2, c3);
+  return c;
+}
+
+__device__ __forceinline__ uint4 philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                          uint32_t k1)
+{
+  return philox_rounds<10>(make_uint4(c0, c1, c2, c3), k0, k1);
 }
 
 // (0, 1] float of a 32-bit draw.  The product is exact (power-of-two scale),

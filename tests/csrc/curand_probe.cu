@@ -46,7 +46,7 @@ __global__ void k_fast_exp(const float* x, float* y, int n)
 __global__ void k_shadow(const double* g, const double* base, float* out, int n)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) out[q] = wlg::shadow_of(g[q], wlg::split_bits(base[q]));
+  if (q < n) out[q] = wlg::shadow_split(g[q], wlg::split_float(base[q]));
 }
 
 // max |__logf(x) - log(x)| over the floats with bit patterns [lo, hi]
