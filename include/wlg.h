@@ -274,6 +274,56 @@ wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out);
 wlg_status wlg_class_log_probs(const int* energies, const double* log_g, const long long* offset, const int* count,
                                int n_classes, double prob, double* log_z, double* log_probs);
 
+/* ---- Serving: continuous batching of decoding requests (no counterpart
+ * in the reference, which runs one fixed batch per process).
+ *
+ * A request is one disorder sample, given as a wlg_problem whose
+ * error_class is ignored: the server runs its four error classes i, v, h, c
+ * and retires the request with the classes' log-probabilities at the
+ * Nishimori temperature (wlg_class_log_probs).  Requests are admitted while
+ * their device memory fits the budget; admitted problems keep their walker
+ * state resident in device memory and advance in short main-run launches
+ * ("epochs") shared with every other resident problem, so requests that
+ * arrive while others run join the next epoch and finished ones leave it.
+ * Each result equals the batch engine's for the same problems.  A server
+ * owns a host thread and CUDA streams on `device`; submit and poll may be
+ * called from any thread. */
+typedef struct wlg_server wlg_server;
+
+typedef struct {
+  size_t mem_budget_bytes; /* device memory for resident problems; 0: 1 GiB */
+  int epoch_outer;         /* outer WL iterations per main-run launch; 0: 4 */
+  int max_prerun_batch;    /* requests per pre-run launch; 0: 256 */
+  int max_resident;        /* resident problems (4 per request); 0: 8192 */
+} wlg_server_config;
+
+typedef struct {
+  unsigned long long id;       /* as returned by wlg_server_submit */
+  int status;                  /* WLG_OK, or the first failing class's status */
+  int pad;
+  long long outer_iterations[4]; /* main-run outer iterations per class i, v, h, c */
+  double log_z[4];             /* log Z_c at beta_N = ln((1-p)/p) / 2 */
+  double log_probs[4];         /* log Z_c - logsumexp_c log Z_c */
+  double submit_ms, done_ms;   /* host clock, milliseconds since the server started */
+} wlg_decoded;
+
+typedef struct {
+  long long submitted, completed, resident_problems, epochs, main_launches, prerun_launches;
+  long long bytes_in_use, bytes_budget;
+} wlg_server_stats;
+
+wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_server** out);
+/* Queues n requests; ids[i] receives request i's id.  Invalid requests are
+ * rejected whole (WLG_ERR_INVALID, nothing queued). */
+wlg_status wlg_server_submit(wlg_server* server, const wlg_problem* requests, int n, unsigned long long* ids);
+/* Up to `cap` finished requests in completion order; waits up to timeout_ms
+ * (0: no wait) for at least one.  *n_out = 0 when none finished in time. */
+wlg_status wlg_server_poll(wlg_server* server, wlg_decoded* out, int cap, int* n_out, int timeout_ms);
+wlg_status wlg_server_stats_get(const wlg_server* server, wlg_server_stats* out);
+/* Stops the loop (unfinished requests are dropped) and frees everything. */
+wlg_status wlg_server_destroy(wlg_server* server);
+const char* wlg_server_last_error(const wlg_server* server);
+
 #ifdef __cplusplus
 }
 #endif

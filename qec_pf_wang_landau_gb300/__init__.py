@@ -50,8 +50,15 @@ SIGNATURES = {
     "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
     "wlg_solve_raw_noalloc": [P, i32, P, P, P, P, i64, P, P],
     "wlg_class_log_probs": [P, P, P, P, i32, f64, P, P],
+    "wlg_server_create": [i32, P, P],
+    "wlg_server_submit": [P, P, i32, P],
+    "wlg_server_poll": [P, P, i32, P, i32],
+    "wlg_server_stats_get": [P, P],
+    "wlg_server_destroy": [P],
+    "wlg_server_last_error": [P],
 }
-_RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p}
+_RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p,
+            "wlg_server_last_error": C.c_char_p}
 
 
 class WlgError(RuntimeError):
@@ -226,3 +233,86 @@ def class_log_probs(curves, prob):
     call("wlg_class_log_probs", E.ctypes.data_as(P), G.ctypes.data_as(P), off.ctypes.data_as(P),
          cnt.ctypes.data_as(P), len(curves), prob, lz.ctypes.data_as(P), lp.ctypes.data_as(P))
     return lz, lp
+
+
+# ----------------------------------------------------------------- serving --
+
+class ServerConfig(C.Structure):
+    _fields_ = [("mem_budget_bytes", sz), ("epoch_outer", i32), ("max_prerun_batch", i32), ("max_resident", i32)]
+
+
+class Decoded(C.Structure):
+    """wlg_decoded: one retired request (classes in the order i, v, h, c)."""
+    _fields_ = [("id", u64), ("status", i32), ("pad", i32), ("outer_iterations", i64 * 4), ("log_z", f64 * 4),
+                ("log_probs", f64 * 4), ("submit_ms", f64), ("done_ms", f64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", i64), ("completed", i64), ("resident_problems", i64), ("epochs", i64),
+                ("main_launches", i64), ("prerun_launches", i64), ("bytes_in_use", i64), ("bytes_budget", i64)]
+
+
+class Server:
+    """Continuous-batching decoder (wlg_server_*): submit disorder samples,
+    poll retired requests with their four class log-probabilities."""
+
+    def __init__(self, device: int = 0, mem_budget_bytes: int = 0, epoch_outer: int = 0, max_prerun_batch: int = 0,
+                 max_resident: int = 0):
+        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident)
+        h = C.c_void_p()
+        call("wlg_server_create", device, C.byref(cfg), C.byref(h))
+        self._h = h
+
+    def submit(self, requests):
+        """Queue requests (Problems; error_class ignored); returns their ids."""
+        n = len(requests)
+        arr = (Problem * n)(*requests)
+        ids = (u64 * max(n, 1))()
+        self._check("wlg_server_submit", lib().wlg_server_submit(self._h, C.cast(arr, P), n, C.cast(ids, P)))
+        return [int(ids[i]) for i in range(n)]
+
+    def poll(self, cap: int = 256, timeout_ms: int = 0):
+        """Up to `cap` retired requests (Decoded), waiting up to timeout_ms for one."""
+        out = (Decoded * cap)()
+        k = i32(0)
+        self._check("wlg_server_poll", lib().wlg_server_poll(self._h, C.cast(out, P), cap, C.byref(k), timeout_ms))
+        return [out[i] for i in range(k.value)]
+
+    def wait(self, ids, timeout_s: float = 600.0):
+        """Poll until every id in `ids` is retired: {id: Decoded}."""
+        import time
+        want, got = set(ids), {}
+        t_end = time.monotonic() + timeout_s
+        while want - set(got):
+            if time.monotonic() > t_end:
+                raise TimeoutError(f"{len(want - set(got))} requests not retired")
+            for d in self.poll(256, 100):
+                got[int(d.id)] = d
+        return {i: got[i] for i in ids}
+
+    def stats(self):
+        st = ServerStats()
+        call("wlg_server_stats_get", self._h, C.byref(st))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def _check(self, name, st):
+        if st != 0:
+            detail = lib().wlg_server_last_error(self._h).decode()
+            raise WlgError(name, st, f"{lib().wlg_status_string(st).decode()}: {detail}")
+
+    def close(self):
+        if self._h:
+            lib().wlg_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,142 @@
+// Batch pipeline internals shared by the batch entry points
+// (wlg_engine_host.cpp) and the serving loop (wlg_server.cpp): where a batch
+// runs, the pre-run -> main-run hand-off, the kernel launchers and result
+// stitching.  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/wlg.h"
+#include "wlg_engine.h"
+
+namespace wlg {
+
+// ---- kernels (wlg_engine.cu)
+wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem, int8_t* Jpool, uint8_t* seen_pool,
+                            int8_t* found_pool, int* fflag_pool, cudaStream_t s);
+int main_batch_capacity(int variant, int cta_threads, int smem);
+wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
+                             int team_bytes, int teams_per_cta, int grid, int* d_next, double* gpool,
+                             long long gslot_doubles, const uint32_t* Jpool, const uint32_t* latpool,
+                             const int* winpool, const uint32_t* maskpool, double* outpool, MainResult* results,
+                             unsigned char* statepool, cudaStream_t s);
+
+// ---- windows and stitching (interval.cpp, result_handling.cpp)
+wlg_status make_windows(int e_min, int e_max, int n, float overlap, std::vector<int>& start, std::vector<int>& end);
+using Curve = std::map<int, double>;
+wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<std::pair<int, double>>& out);
+
+// Stitched, normalised (E, log g) of one finished problem from its compact
+// walker-0 output out[I][L] and its windows win[5 I] (start, end, base, Lb, E0).
+wlg_status stitched_curve(const MainDesc& d, const double* out, const int* win,
+                          std::vector<std::pair<int, double>>& res);
+
+// ---- where a batch runs
+// Device buffers of one batch, by role.
+enum Slot {
+  kPreDesc,
+  kJ8,
+  kSeen,
+  kFound,
+  kFflag,
+  kMainDesc,
+  kOrder,
+  kNext,
+  kJw,
+  kLatw,
+  kWin,
+  kMask,
+  kOut,
+  kRes,
+  kGpool,
+  kSlots
+};
+
+// A stream, a provider of device buffers, optional timing events, and what
+// the batch did.
+struct Exec {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t* ev = nullptr;  // 4 events, or nullptr for no timing
+  float t_pre = 0, t_main = 0;
+  double t_handoff = 0;
+  long long h2d = 0, d2h = 0;
+  int launches = 0;
+  int main_forms = 0;  // bit v: a main-run launch of form v
+  std::string err;
+  virtual ~Exec() = default;
+  // device buffer for `slot` of at least `bytes` bytes
+  virtual wlg_status buffer(Slot slot, size_t bytes, void** out) = 0;
+};
+
+inline wlg_status fail(Exec& ex, wlg_status st, const std::string& msg)
+{
+  ex.err = msg;
+  return st;
+}
+
+template <typename T>
+wlg_status upload(Exec& ex, Slot slot, const std::vector<T>& h, void** dptr)
+{
+  const size_t bytes = h.size() * sizeof(T);
+  wlg_status st = ex.buffer(slot, bytes, dptr);
+  if (st != WLG_OK || bytes == 0) return st;
+  const cudaError_t e = cudaMemcpyAsync(*dptr, h.data(), bytes, cudaMemcpyHostToDevice, ex.stream);
+  ex.h2d += static_cast<long long>(bytes);
+  return e == cudaSuccess ? WLG_OK : fail(ex, WLG_ERR_CUDA, cudaGetErrorString(e));
+}
+
+template <typename T>
+wlg_status download(Exec& ex, const void* dptr, std::vector<T>& h)
+{
+  if (h.empty()) return WLG_OK;
+  const cudaError_t e = cudaMemcpyAsync(h.data(), dptr, h.size() * sizeof(T), cudaMemcpyDeviceToHost, ex.stream);
+  ex.d2h += static_cast<long long>(h.size() * sizeof(T));
+  return e == cudaSuccess ? WLG_OK : fail(ex, WLG_ERR_CUDA, cudaGetErrorString(e));
+}
+
+inline int round32(int x) { return (x + 31) / 32 * 32; }
+
+wlg_status check_problem(const wlg_problem& q);
+
+struct Prepared {
+  std::vector<MainDesc> main;                  // problems that reach the main run
+  std::vector<int> main_problem;               // index into the batch
+  std::vector<std::vector<int>> starts, ends;  // per batch problem
+  std::vector<int> lg, base_off;               // per main entry: log2 step, offset of w_base in win pool
+};
+
+// Main-run inputs of a prepared batch, on the host: packed couplings, start
+// lattices, spectrum masks (32-bit words), windows, and the size of the
+// walker-0 output; MainDesc offsets index these arrays.
+struct Handoff {
+  std::vector<uint32_t> Jw, latw, maskw;
+  std::vector<int> win;
+  long long n_out = 0;
+};
+
+// Validation, the pre-run of every problem (one launch) and the hand-off to
+// the main run on the host.  Problems that cannot start the main run get
+// their status in `results` and no MainDesc.
+wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho);
+
+// Main-run form of a problem by lattice storage: 0 spins in shared memory,
+// 1 spins in a register, 2 register spins + neighbour table (X, Y >= 3);
+// form 3 (FP64 log g in global memory) replaces 0 when the team's state
+// exceeds shared memory.
+inline int main_form(const MainDesc& d) { return d.N > 64 ? 0 : (d.X >= 3 && d.Y >= 3 ? 2 : 1); }
+
+// Shared-memory bytes of a team running d in form `form`.
+inline int team_bytes(const MainDesc& d, int form, int team)
+{
+  return align16(team_layout(team, d.L, d.nwL, d.nwM, d.I, form == 1 || form == 2, form == 2 ? d.N : 0, form != 3)
+                     .bytes +
+                 16);
+}
+
+}  // namespace wlg

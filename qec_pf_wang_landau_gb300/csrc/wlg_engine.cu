@@ -278,14 +278,18 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
                             const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
                             const int* __restrict__ winpool, const uint32_t* __restrict__ maskpool,
                             double* __restrict__ outpool, MainResult* __restrict__ results,
-                            uint32_t* __restrict__ dumppool)
+                            unsigned char* __restrict__ statepool)
 {
   const int P = team.size;
+  // resumable run: state saved at the end of a launch, restored at the start
+  unsigned char* const st = d.off_state >= 0 ? statepool + d.off_state : nullptr;
+  const StateLayout sl = state_layout(P, d.I, d.nwL, d.L);
   const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg, kTable ? d.N : 0, !kGlobalG);
   // FP64 log g: in the team's shared memory, or (large problems) in this
   // resident team's slice of a global pool, L2-resident and touched only on
   // bin changes, averaging and exchange
-  double* G = kGlobalG ? gslot : reinterpret_cast<double*>(base + lay.off_G);
+  double* G = kGlobalG ? (st != nullptr ? reinterpret_cast<double*>(st + sl.off_G) : gslot)
+                       : reinterpret_cast<double*>(base + lay.off_G);
   float* Gf = reinterpret_cast<float*>(base + lay.off_Gf);
   uint32_t* H = reinterpret_cast<uint32_t*>(base + lay.off_H);
   uint32_t* lat_s = reinterpret_cast<uint32_t*>(base + lay.off_lat);
@@ -314,8 +318,9 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     cond[q] = 0;
     flat[q] = 0;
   }
+  const bool resumed = st != nullptr && reinterpret_cast<const int*>(st)[4] != 0;
   for (int c = 0; c < d.L; ++c) {
-    G[c * P + t] = 0.0;
+    if (!resumed || !kGlobalG) G[c * P + t] = 0.0;
     Gf[c * P + t] = 0.0f;
     H[c * P + t] = 0u;
   }
@@ -385,6 +390,34 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   long long outer = 0;
   long long counter = 1;
   int status = WLG_OK;
+  if (resumed) {
+    const long long* hdr = reinterpret_cast<const long long*>(st);
+    outer = hdr[0];
+    counter = hdr[1];
+    if (t < I) {
+      fwin[t] = reinterpret_cast<const double*>(st + sl.off_f)[t];
+      cond[t] = reinterpret_cast<const int*>(st + sl.off_cond)[t];
+    }
+    perm[t] = reinterpret_cast<const int*>(st + sl.off_perm)[t];
+    if (live) {
+      E = reinterpret_cast<const int*>(st + sl.off_E)[t];
+      rng.init(d.key_wl, static_cast<uint64_t>(t), reinterpret_cast<const unsigned long long*>(st + sl.off_pos)[t]);
+      const uint32_t* ls = reinterpret_cast<const uint32_t*>(st + sl.off_lat);
+      if constexpr (kReg) {
+        lt.r = ls[t] | (d.nwL > 1 ? static_cast<uint64_t>(ls[P + t]) << 32 : 0ull);
+      } else {
+        for (int q = 0; q < d.nwL; ++q) lat_s[q * P + t] = ls[q * P + t];
+      }
+    }
+    const uint32_t* hs = reinterpret_cast<const uint32_t*>(st + sl.off_H);
+    const double* gs = reinterpret_cast<const double*>(st + sl.off_G);
+    for (int c = 0; c < d.L; ++c) {
+      H[c * P + t] = hs[c * P + t];
+      if constexpr (!kGlobalG) G[c * P + t] = gs[c * P + t];
+    }
+  }
+  int launch_outer = 0;  // outer iterations of this launch
+  bool suspended = false;
   team.sync();
 
   for (;;) {
@@ -667,39 +700,65 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     if (d.exch_mode == 1) ++counter;
     team.sync();
     if (stop) break;
+    if (st != nullptr && d.epoch_outer > 0 && ++launch_outer >= d.epoch_outer) {
+      suspended = true;
+      break;
+    }
+  }
+
+  if (suspended) {  // save the state; the next launch resumes from it
+    if (t == 0) {
+      long long* hdr = reinterpret_cast<long long*>(st);
+      hdr[0] = outer;
+      hdr[1] = counter;
+      reinterpret_cast<int*>(st)[4] = 1;
+    }
+    if (t < I) {
+      reinterpret_cast<double*>(st + sl.off_f)[t] = fwin[t];
+      reinterpret_cast<int*>(st + sl.off_cond)[t] = cond[t];
+    }
+    reinterpret_cast<int*>(st + sl.off_perm)[t] = perm[t];
+    if (live) {
+      reinterpret_cast<int*>(st + sl.off_E)[t] = E;
+      reinterpret_cast<unsigned long long*>(st + sl.off_pos)[t] = rng.pos;
+      uint32_t* ls = reinterpret_cast<uint32_t*>(st + sl.off_lat);
+      for (int q = 0; q < d.nwL; ++q) {
+        if constexpr (kReg) {
+          ls[q * P + t] = static_cast<uint32_t>(lt.r >> (32 * q));
+        } else {
+          ls[q * P + t] = lat_s[q * P + t];
+        }
+      }
+    }
+    uint32_t* hs = reinterpret_cast<uint32_t*>(st + sl.off_H);
+    double* gs = reinterpret_cast<double*>(st + sl.off_G);
+    for (int c = 0; c < d.L; ++c) {
+      hs[c * P + t] = H[c * P + t];
+      if constexpr (!kGlobalG) gs[c * P + t] = G[c * P + t];
+    }
+    if (t == 0) {
+      MainResult r{};
+      r.status = WLG_OK;
+      r.outer = outer;
+      r.flips = outer * static_cast<long long>(d.nwalk) * d.n_iter;
+      r.done = 0;
+      results[p] = r;
+    }
+    team.sync();
+    return;
   }
 
   // ---- results
   if (live && w == 0) {
     for (int c = 0; c < d.L; ++c) outpool[d.off_out + static_cast<long long>(b) * d.L + c] = G[c * P + t];
   }
-  if (d.off_dump >= 0 && live) {
-    const long long per = dump_words_per_walker(d.nwL, d.L);
-    uint32_t* o = dumppool + d.off_dump + per * t;
-    o[0] = static_cast<uint32_t>(E);
-    o[1] = static_cast<uint32_t>(rng.pos);
-    o[2] = static_cast<uint32_t>(rng.pos >> 32);
-    for (int q = 0; q < d.nwL; ++q) {
-      if constexpr (kReg) {
-        o[3 + q] = static_cast<uint32_t>(lt.r >> (32 * q));
-      } else {
-        o[3 + q] = lat_s[q * P + t];
-      }
-    }
-    for (int c = 0; c < d.L; ++c) {
-      const double g = G[c * P + t];
-      const unsigned long long gb = static_cast<unsigned long long>(__double_as_longlong(g));
-      o[3 + d.nwL + 2 * c] = static_cast<uint32_t>(gb);
-      o[3 + d.nwL + 2 * c + 1] = static_cast<uint32_t>(gb >> 32);
-      o[3 + d.nwL + 2 * d.L + c] = H[c * P + t];
-    }
-  }
   if (t == 0) {
-    MainResult r;
+    MainResult r{};
     r.status = status;
     r.new_energy = misc[2];
     r.outer = outer;
     r.flips = outer * static_cast<long long>(d.nwalk) * d.n_iter;
+    r.done = 1;
     results[p] = r;
   }
   team.sync();
@@ -714,7 +773,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __re
                                                      const int* __restrict__ winpool,
                                                      const uint32_t* __restrict__ maskpool,
                                                      double* __restrict__ outpool, MainResult* __restrict__ results,
-                                                     uint32_t* __restrict__ dumppool)
+                                                     unsigned char* __restrict__ statepool)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tix = threadIdx.x / team_size;
@@ -730,10 +789,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __re
     if (q >= n) return;
     const int p = order[q];
     const MainDesc d = descs[p];
+    if (d.off_state >= 0 && results[p].done != 0) continue;  // resumable run that finished in an earlier launch
     double* gslot = kGlobalG ? gpool + (static_cast<long long>(blockIdx.x) * (blockDim.x / team_size) + tix) * gslot_doubles
                              : nullptr;
     run_problem<kReg, kTable, kGlobalG>(d, p, team, t, base, gslot, Jpool, latpool, winpool, maskpool, outpool, results,
-                                        dumppool);
+                                        statepool);
   }
 }
 
@@ -754,7 +814,7 @@ wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem
 }
 
 using MainFn = void (*)(const MainDesc*, const int*, int, int, int, int*, double*, long long, const uint32_t*,
-                        const uint32_t*, const int*, const uint32_t*, double*, MainResult*, uint32_t*);
+                        const uint32_t*, const int*, const uint32_t*, double*, MainResult*, unsigned char*);
 
 // variant: 0 = spins and log g in shared memory, 1 = spins in a register,
 // 2 = register spins + neighbour table, 3 = spins in shared memory, FP64 log g
@@ -795,7 +855,7 @@ wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_
                              int team_bytes, int teams_per_cta, int grid, int* d_next, double* gpool,
                              long long gslot_doubles, const uint32_t* Jpool,
                              const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
-                             MainResult* results, uint32_t* dumppool, cudaStream_t s)
+                             MainResult* results, unsigned char* statepool, cudaStream_t s)
 {
   if (n == 0) return WLG_OK;
   const int threads = team_size * teams_per_cta;
@@ -803,7 +863,7 @@ wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_
   MainFn fn = main_fn(variant, threads);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return WLG_ERR_CUDA;
   fn<<<grid, threads, smem, s>>>(d_descs, d_order, n, team_size, team_bytes, d_next, gpool, gslot_doubles, Jpool,
-                                 latpool, winpool, maskpool, outpool, results, dumppool);
+                                 latpool, winpool, maskpool, outpool, results, statepool);
   return launch_status();
 }
 

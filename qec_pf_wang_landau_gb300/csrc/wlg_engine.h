@@ -59,16 +59,54 @@ struct MainDesc {
   long long off_win;             // ints: start[I], end[I], base[I], Lb[I], E0[I]
   long long off_mask;            // words [nwM]
   long long off_out;             // doubles: [I][L] walker-0 log g (compact)
-  long long off_dump;            // per-walker dump slot (tests), -1 = none
+  long long off_state;           // bytes: saved state (state_layout) of a resumable run, -1 = run to the end
+  int epoch_outer;               // resumable runs: outer iterations per launch before the state is saved
 };
 
-// Per-problem result of the main run.
+// Per-problem result of the main run (of one launch, for resumable runs).
 struct MainResult {
   int status;  // WLG_OK, WLG_ERR_NEW_ENERGY, WLG_ERR_TIMEOUT
   int new_energy;
   long long outer;
   long long flips;
+  int done;    // 1: finished (status final, log g written); 0: suspended
+  int pad;
 };
+
+// Saved state of a suspended problem (resumable runs), byte offsets: a
+// header (outer iterations, exchange counter, started flag), per window
+// f and cond, per walker the exchange permutation, energy, RNG position,
+// lattice words, compact histogram [L] and FP64 log g [L] (interleaved
+// [bin][walker] like the team's shared memory).
+struct StateLayout {
+  long long off_f, off_cond, off_perm, off_E, off_pos, off_lat, off_H, off_G, bytes;
+};
+
+WLG_HD inline long long align8(long long x) { return (x + 7) & ~7ll; }
+
+WLG_HD inline StateLayout state_layout(int P, int I, int nwL, int L)
+{
+  StateLayout s{};
+  long long o = 32;  // header: long long outer, long long counter, int started
+  s.off_f = o;
+  o += 8ll * I;
+  s.off_cond = o;
+  o = align8(o + 4ll * I);
+  s.off_perm = o;
+  o = align8(o + 4ll * P);
+  s.off_E = o;
+  o = align8(o + 4ll * P);
+  s.off_pos = o;
+  o += 8ll * P;
+  s.off_lat = o;
+  o = align8(o + 4ll * nwL * P);
+  s.off_H = o;
+  o = align8(o + 4ll * L * P);
+  s.off_G = o;
+  o += 8ll * L * P;
+  s.bytes = o;
+  return s;
+}
 
 // Team shared-memory layout of a problem (bytes, 16-byte aligned pieces).
 struct TeamLayout {
@@ -118,9 +156,5 @@ WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, b
   t.bytes = o;
   return t;
 }
-
-// Dump of one problem's final walker state (parity tests), per walker:
-// E, RNG position, lattice words, then the compact log g [L] and H [L].
-WLG_HD inline long long dump_words_per_walker(int nwL, int L) { return 1 + 2 + nwL + 2 * L + L; }
 
 }  // namespace wlg

@@ -18,20 +18,12 @@
 #include <vector>
 
 #include "../../include/wlg.h"
+#include "wlg_batch.h"
 #include "wlg_engine.h"
 #include "wlg_internal.h"
 #include "wlg_keys.h"
 
 namespace wlg {
-
-wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem, int8_t* Jpool, uint8_t* seen_pool,
-                            int8_t* found_pool, int* fflag_pool, cudaStream_t s);
-int main_batch_capacity(int variant, int cta_threads, int smem);
-wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
-                             int team_bytes, int teams_per_cta, int grid, int* d_next, double* gpool,
-                             long long gslot_doubles, const uint32_t* Jpool,
-                             const uint32_t* latpool, const int* winpool, const uint32_t* maskpool, double* outpool,
-                             MainResult* results, uint32_t* dumppool, cudaStream_t s);
 
 // ---------------------------------------------------------- energy windows --
 // interval.cpp:5-41: window length from a float division truncated toward
@@ -78,8 +70,6 @@ int energy_host(const int8_t* s, const int8_t* J, int X, int Y, int boundary)
 }
 
 // ----------------------------------------------------------------- stitching --
-
-using Curve = std::map<int, double>;
 
 std::tuple<int, double> best_shared_key(const Curve& a, const Curve& b)
 {
@@ -201,7 +191,26 @@ wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<
   return WLG_OK;
 }
 
+// result_handling.cpp:368-431 applied to the compact walker-0 output of one
+// problem: each window's reachable energies with nonzero log g.
+wlg_status stitched_curve(const MainDesc& d, const double* out, const int* win,
+                          std::vector<std::pair<int, double>>& res)
+{
+  const int g = 1 << d.lg;
+  std::vector<Curve> curves(static_cast<size_t>(d.I));
+  for (int b = 0; b < d.I; ++b) {
+    const int base = win[2 * d.I + b], len = win[3 * d.I + b];
+    for (int c = 0; c < len; ++c) {
+      const double v = out[static_cast<long long>(b) * d.L + c];
+      if (v != 0) curves[b].emplace(base + c * g, v);
+    }
+  }
+  return stitch_windows(std::move(curves), d.X, d.Y, res);
+}
+
 }  // namespace wlg
+
+using namespace wlg;
 
 // ------------------------------------------------------------------ context --
 
@@ -210,25 +219,6 @@ struct DevBuf {
   size_t cap = 0;
 };
 
-// Device buffers of one batch, by role.
-enum Slot {
-  kPreDesc,
-  kJ8,
-  kSeen,
-  kFound,
-  kFflag,
-  kMainDesc,
-  kOrder,
-  kNext,
-  kJw,
-  kLatw,
-  kWin,
-  kMask,
-  kOut,
-  kRes,
-  kGpool,
-  kSlots
-};
 
 struct wlg_context {
   int device = 0;
@@ -246,33 +236,6 @@ struct wlg_context {
 };
 
 namespace {
-
-using wlg::MainDesc;
-using wlg::MainResult;
-using wlg::PreDesc;
-
-// Where a batch runs: its stream, a provider of device buffers, optional
-// timing events, and what it did.
-struct Exec {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t* ev = nullptr;  // 4 events, or nullptr for no timing
-  float t_pre = 0, t_main = 0;
-  double t_handoff = 0;
-  long long h2d = 0, d2h = 0;
-  int launches = 0;
-  int main_forms = 0;  // bit v: a main-run launch of form v
-  std::string err;
-  virtual ~Exec() = default;
-  // device buffer for `slot` of at least `bytes` bytes
-  virtual wlg_status buffer(Slot slot, size_t bytes, void** out) = 0;
-};
-
-wlg_status fail(Exec& ex, wlg_status st, const std::string& msg)
-{
-  ex.err = msg;
-  return st;
-}
 
 wlg_status grow(wlg_context* ctx, DevBuf& b, size_t bytes, std::string& err)
 {
@@ -315,27 +278,9 @@ struct ContextExec final : Exec {
   }
 };
 
-template <typename T>
-wlg_status upload(Exec& ex, Slot slot, const std::vector<T>& h, void** dptr)
-{
-  const size_t bytes = h.size() * sizeof(T);
-  wlg_status st = ex.buffer(slot, bytes, dptr);
-  if (st != WLG_OK || bytes == 0) return st;
-  const cudaError_t e = cudaMemcpyAsync(*dptr, h.data(), bytes, cudaMemcpyHostToDevice, ex.stream);
-  ex.h2d += static_cast<long long>(bytes);
-  return e == cudaSuccess ? WLG_OK : fail(ex, WLG_ERR_CUDA, cudaGetErrorString(e));
-}
+}  // namespace
 
-template <typename T>
-wlg_status download(Exec& ex, const void* dptr, std::vector<T>& h)
-{
-  if (h.empty()) return WLG_OK;
-  const cudaError_t e = cudaMemcpyAsync(h.data(), dptr, h.size() * sizeof(T), cudaMemcpyDeviceToHost, ex.stream);
-  ex.d2h += static_cast<long long>(h.size() * sizeof(T));
-  return e == cudaSuccess ? WLG_OK : fail(ex, WLG_ERR_CUDA, cudaGetErrorString(e));
-}
-
-int round32(int x) { return (x + 31) / 32 * 32; }
+namespace wlg {
 
 wlg_status check_problem(const wlg_problem& q)
 {
@@ -351,17 +296,9 @@ wlg_status check_problem(const wlg_problem& q)
   return WLG_OK;
 }
 
-struct Prepared {
-  std::vector<MainDesc> main;          // problems that reach the main run
-  std::vector<int> main_problem;       // index into the batch
-  std::vector<std::vector<int>> starts, ends;  // per batch problem
-  std::vector<int> lg, base_off;       // per main entry: log2 step, offset of w_base in win pool
-};
-
-// The whole batch up to the main-run results.
-wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results,
-                     std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
-                     std::vector<int>& win_host)
+// Validation, the pre-run of every problem (one launch) and the hand-off to
+// the main run on the host.
+wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho)
 {
   using clock = std::chrono::steady_clock;
   ex.h2d = ex.d2h = 0;
@@ -437,8 +374,14 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
 
   // ---------------- hand-off (file_io.cpp:558-659, mainrun.cu:79-113)
   const auto t0 = clock::now();
-  std::vector<uint32_t> Jw, latw, maskw;
-  std::vector<int> win;
+  std::vector<uint32_t>& Jw = ho.Jw;
+  std::vector<uint32_t>& latw = ho.latw;
+  std::vector<uint32_t>& maskw = ho.maskw;
+  std::vector<int>& win = ho.win;
+  Jw.clear();
+  latw.clear();
+  maskw.clear();
+  win.clear();
   long long o_out = 0;
   prep.starts.assign(static_cast<size_t>(n), {});
   prep.ends.assign(static_cast<size_t>(n), {});
@@ -575,12 +518,34 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
     }
     d.off_out = o_out;
     o_out += static_cast<long long>(d.I) * d.L;
-    d.off_dump = -1;
+    d.off_state = -1;
+    d.epoch_outer = 0;
     prep.main.push_back(d);
     prep.main_problem.push_back(p);
     prep.lg.push_back(lg);
   }
   ex.t_handoff = std::chrono::duration<double, std::milli>(clock::now() - t0).count();
+  ho.n_out = o_out;
+  return WLG_OK;
+}
+
+}  // namespace wlg
+
+namespace {
+
+// The whole batch up to the main-run results.
+wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results,
+                     std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
+                     std::vector<int>& win_host)
+{
+  Handoff ho;
+  wlg_status st = wlg::prepare_batch(ex, probs, n, results, prep, ho);
+  if (st != WLG_OK) return st;
+  const std::vector<uint32_t>& Jw = ho.Jw;
+  const std::vector<uint32_t>& latw = ho.latw;
+  const std::vector<uint32_t>& maskw = ho.maskw;
+  const std::vector<int>& win = ho.win;
+  const long long o_out = ho.n_out;
 
   // ---------------- main run: one persistent launch per (lattice storage, team size)
   const int m = static_cast<int>(prep.main.size());
@@ -827,7 +792,6 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
   if (st != WLG_OK) return st;
   const auto t0 = std::chrono::steady_clock::now();
   long long pos = 0;
-  std::vector<double> dense;
   for (size_t i = 0; i < prep.main.size(); ++i) {
     const int p = prep.main_problem[i];
     wlg_result& r = results[p];
@@ -835,15 +799,8 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
     r.n_energies = 0;
     if (r.status != WLG_OK) continue;
     const MainDesc& d = prep.main[i];
-    std::vector<wlg::Curve> curves(static_cast<size_t>(d.I));
-    for (int b = 0; b < d.I; ++b) {
-      dense_window(d, out, win, b, dense);
-      const int s = win[d.off_win + b];
-      for (size_t k = 0; k < dense.size(); ++k)
-        if (dense[k] != 0) curves[b].emplace(s + static_cast<int>(k), dense[k]);
-    }
     std::vector<std::pair<int, double>> res;
-    const wlg_status sst = wlg::stitch_windows(std::move(curves), d.X, d.Y, res);
+    const wlg_status sst = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, res);
     if (sst != WLG_OK) {
       r.status = sst;
       continue;

@@ -53,8 +53,11 @@ def test_struct_layouts_match_c(engine, tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
+    structs = ((engine.Problem, "wlg_problem"), (engine.Result, "wlg_result"), (engine.Stats, "wlg_stats"),
+               (engine.ServerConfig, "wlg_server_config"), (engine.Decoded, "wlg_decoded"),
+               (engine.ServerStats, "wlg_server_stats"))
     lines = []
-    for cls, cname in ((engine.Problem, "wlg_problem"), (engine.Result, "wlg_result")):
+    for cls, cname in structs:
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
         for f, _ in cls._fields_:
             lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
@@ -65,7 +68,7 @@ def test_struct_layouts_match_c(engine, tmp_path):
     subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                         check=True).stdout.splitlines())
-    for cls, cname in ((engine.Problem, "wlg_problem"), (engine.Result, "wlg_result")):
+    for cls, cname in structs:
         assert int(got[cname]) == C.sizeof(cls)
         for f, _ in cls._fields_:
             assert int(got[f"{cname}.{f}"]) == getattr(cls, f).offset, f
@@ -79,3 +82,17 @@ def test_invalid_arguments_rejected_without_gpu(engine):
     assert L.wlg_wang_landau(*([None] * 17), 4, 4, 10, 30, 7, 30, 1, 0, None) == 1  # walkers % intervals != 0
     out = C.c_void_p()
     assert L.wlg_context_create(-1, 0, C.byref(out)) == 1
+    assert L.wlg_server_create(0, None, None) == 1
+    assert L.wlg_server_submit(None, None, 0, None) == 1
+    assert L.wlg_server_poll(None, None, 0, None, 0) == 1
+    assert L.wlg_server_destroy(None) == 1
+
+
+def test_server_without_a_device_fails_cleanly(engine):
+    """Creating a server where no GPU is visible returns WLG_ERR_CUDA (2)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    out = C.c_void_p()
+    assert engine.lib().wlg_server_create(0, None, C.byref(out)) == 2
+    assert out.value is None
