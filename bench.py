@@ -112,6 +112,113 @@ def reference_cuda_run():
     return conv / (tot_ms / 1e3), tot_ms / 1e3
 
 
+SERVING = dict(rate=200.0, seconds=1.0, side_min=4, side_max=16, prob_min=0.02, prob_max=0.12, beta=1e-6,
+               walkers_per_interval=4, wait_s=120.0, seed=2026)
+
+
+def serving_requests(n_max: int = 100000):
+    """Poisson arrival times and decoding requests of the serving workload:
+    square periodic lattices with side uniform in {4..16}, p uniform in
+    [0.02, 0.12], ln f 1e-6, windows scaled with N (N/16, 4..16), 4 walkers
+    each, pre-run 128 walkers x 100 N iterations; all four classes per
+    request (the server runs them)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = SERVING
+    rng = np.random.default_rng(c["seed"])
+    t, arrivals, reqs = 0.0, [], []
+    while len(reqs) < n_max:
+        t += rng.exponential(1.0 / c["rate"])
+        if t > c["seconds"]:
+            break
+        L = int(rng.integers(c["side_min"], c["side_max"] + 1))
+        N = L * L
+        arrivals.append(t)
+        reqs.append(wlg.problem(L, L, prob=float(rng.uniform(c["prob_min"], c["prob_max"])), seed=c["seed"],
+                                sample=len(reqs), pre_walkers=128, pre_intervals=32, pre_iterations=100 * N,
+                                intervals=int(min(16, max(4, N // 16))), walkers_per_interval=c["walkers_per_interval"],
+                                overlap=0.25, alpha=0.8, beta=c["beta"], iterations=1000, exchange_every=10))
+    return arrivals, reqs
+
+
+def serving_run():
+    """The serving workload through wlg_server: requests submitted at their
+    Poisson arrival times, latency = retirement - submission (server clock)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    arrivals, reqs = serving_requests()
+    got, ids = {}, []
+    with wlg.Server(0) as srv:
+        t0 = time.perf_counter()
+        for a, q in zip(arrivals, reqs):
+            delay = t0 + a - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids += srv.submit([q])
+            for d in srv.poll(256, 0):
+                got[int(d.id)] = d
+        while len(got) < len(ids) and time.perf_counter() - t0 < SERVING["wait_s"]:
+            for d in srv.poll(256, 50):
+                got[int(d.id)] = d
+        st = srv.stats()
+    done = [got[i] for i in ids if i in got]
+    lat = np.array([d.done_ms - d.submit_ms for d in done]) if done else np.zeros(1)
+    span_s = (max(d.done_ms for d in done) - min(d.submit_ms for d in done)) / 1e3 if done else float("nan")
+    statuses = {}
+    for d in done:
+        statuses[str(d.status)] = statuses.get(str(d.status), 0) + 1
+    return {"workload": "Poisson 200 req/s for 1 s, side U{4..16} periodic, p U[0.02,0.12], ln f 1e-6, "
+                        "4 classes per request, W=4, I=N/16 in [4,16]",
+            "requests": len(ids), "retired": len(done), "retired_ok": statuses.get("0", 0), "status_counts": statuses,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "throughput_req_s": len(done) / span_s if done else 0.0,
+            "epochs": st["epochs"], "prerun_launches": st["prerun_launches"],
+            "note": f"requests not retired within {SERVING['wait_s']:.0f} s are left out of the percentiles"}
+
+
+BATCHED = dict(samples=2000, sides=(4, 6, 8, 10, 12), prob_min=0.02, prob_max=0.12, beta=1e-6, seed=31337)
+
+
+def batched_problems():
+    """The heterogeneous batched workload: 2000 disorder samples, side
+    uniform in {4,6,8,10,12}, boundary periodic/open 50/50, p uniform in
+    [0.02, 0.12], class uniform over i/v/h/c, windows 8..32 scaled with N,
+    4 walkers each, overlap 0.25, flatness 0.8, ln f 1e-6; per-sample
+    parameters from a seeded host generator, disorder from Philox."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = BATCHED
+    rng = np.random.default_rng(c["seed"])
+    out = []
+    for k in range(c["samples"]):
+        L = int(rng.choice(c["sides"]))
+        N = L * L
+        out.append(wlg.problem(L, L, boundary=int(rng.integers(0, 2)), prob=float(rng.uniform(c["prob_min"], c["prob_max"])),
+                               error_class="ivhc"[int(rng.integers(0, 4))], seed=c["seed"], sample=k, pre_walkers=128,
+                               pre_intervals=32, pre_iterations=100 * N, intervals=int(min(32, max(8, N // 8))),
+                               walkers_per_interval=4, overlap=0.25, alpha=0.8, beta=c["beta"], iterations=1000,
+                               exchange_every=10))
+    return out
+
+
+def batched_run():
+    """The heterogeneous batch in one wlg_solve call: converged samples/s."""
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = batched_problems()
+    ctx = wlg.Context(0)
+    t0 = time.perf_counter()
+    out = ctx.solve(probs)
+    wall = time.perf_counter() - t0
+    st = ctx.stats()
+    dev_s = (st["pre_ms"] + st["handoff_ms"] + st["main_ms"]) / 1e3
+    counts = {}
+    for r, _, _ in out:
+        counts[str(r.status)] = counts.get(str(r.status), 0) + 1
+    flips = sum(r.flips for r, _, _ in out)
+    return {"workload": "2000 samples, side U{4,6,8,10,12}, open/periodic 50/50, p U[0.02,0.12], class U{ivhc}, "
+                        "I = N/8 in [8,32], W=4, o=0.25, alpha=0.8, ln f 1e-6, exchange every 10",
+            "value": counts.get("0", 0) / dev_s, "unit": "samples/s", "e2e_samples_per_s": counts.get("0", 0) / wall,
+            "status_counts": counts, "flips_per_s": flips / (st["main_ms"] / 1e3), "pre_ms": st["pre_ms"],
+            "main_ms": st["main_ms"], "main_forms": st["main_forms"], "kernel_launches": st["kernel_launches"]}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -173,6 +280,18 @@ def flush_l2(torch, buf):
     buf.add_(1)  # 512 MiB read+write, far beyond the 129 MB L2
 
 
+def reduce_over_ranks(dist, times, counts, device):
+    """Whole-job figures of a sharded run: the slowest rank's times, the
+    sum of every rank's counts (samples, flips).  No data-path collective:
+    ranks solve disjoint samples and meet only here."""
+    import torch
+    tt = torch.tensor(times, dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    cc = torch.tensor(counts, dtype=torch.float64, device=device)
+    dist.all_reduce(cc, op=dist.ReduceOp.SUM)
+    return tt.tolist(), [int(v) for v in cc.tolist()]
+
+
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
@@ -223,12 +342,8 @@ def run_ours(args):
     t_e2e = sum(e2e_s)
     t_main = sum(main_ms) / 1e3
     if dist is not None:
-        tt = torch.tensor([t_dev, t_e2e, t_main], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, t_e2e, t_main = tt.tolist()
-        cc = torch.tensor([converged, flips], dtype=torch.float64, device="cuda")
-        dist.all_reduce(cc, op=dist.ReduceOp.SUM)
-        converged, flips = int(cc[0].item()), int(cc[1].item())
+        (t_dev, t_e2e, t_main), (converged, flips) = reduce_over_ranks(dist, [t_dev, t_e2e, t_main],
+                                                                       [converged, flips], "cuda")
     if rank != 0:
         return None
     peaks, peak_kind = measured_peaks()
@@ -274,6 +389,9 @@ def run_ours(args):
                                           "advances, so it runs without replica exchange at -c 20"}
     if clocks is not None:
         line["clocks"] = clocks
+    if not args.no_extra:
+        line["batched"] = batched_run()
+        line["serving"] = serving_run()
     return line
 
 
@@ -343,9 +461,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--profile-case", default=None, help="run a small fixed case for a profiler and exit")
+    ap.add_argument("--leg", default=None, choices=["serving", "batched"], help="run one extra leg alone and print it")
+    ap.add_argument("--no-extra", action="store_true", help="skip the serving and batched legs")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args.profile_case)
+        return
+    if args.leg is not None:
+        import qec_pf_wang_landau_gb300 as wlg
+        wlg.build()
+        print(json.dumps({args.leg: serving_run() if args.leg == "serving" else batched_run()}), flush=True)
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
