@@ -240,6 +240,30 @@ wlg_status wlg_solve_raw_noalloc(const wlg_problem* problems, int n, wlg_result*
                                  int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset,
                                  wlg_stream stream);
 
+/* The pre-run alone (prerun.cu:36-154) for a batch of problems (their
+ * main-run fields are ignored): what the reference writes to
+ * prerun_results.h5 (file_io.cpp:23-192).  Outputs are concatenated in
+ * problem order; for problem p with N = X*Y and B = pre_intervals:
+ *   seen[4N+1]          1 where the pre-run visited energy -2N + i, else 0
+ *                       (the /Histogram/<k> dataset);
+ *   couplings[2N]       +-1 after the error class (/Interaction/<k>);
+ *   found[B], found_energy[B], lattices[B][N]: per coarse bin whether a
+ *                       lattice was stored, its energy and spins +-1
+ *                       (/Lattice/<k>/<E>).
+ * Any output pointer may be NULL. */
+wlg_status wlg_prerun(wlg_context* ctx, const wlg_problem* problems, int n, unsigned char* seen,
+                      signed char* couplings, int* found, int* found_energy, signed char* lattices);
+
+/* The main run and stitching (mainrun.cu:36-421) from pre-run outputs in
+ * the layout wlg_prerun writes (the reference's mainrun reading
+ * prerun_results.h5).  time_limit_s > 0 stops unfinished problems with
+ * WLG_ERR_TIMEOUT once it passes (checked every 4 outer iterations; the
+ * reference checks after each, mainrun.cu:376-383).  Results as wlg_solve. */
+wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, const unsigned char* seen,
+                       const signed char* couplings, const int* found, const int* found_energy,
+                       const signed char* lattices, double time_limit_s, wlg_result* results, int* energies,
+                       double* log_g, long long capacity);
+
 /* Plain form: the same problems computed with the reference's own structure
  * (prerun.cu:36-154, mainrun.cu:115-421) on the operators above — one
  * launch per operation, one thread per walker, state in global memory,
@@ -323,6 +347,20 @@ wlg_status wlg_server_stats_get(const wlg_server* server, wlg_server_stats* out)
 /* Stops the loop (unfinished requests are dropped) and frees everything. */
 wlg_status wlg_server_destroy(wlg_server* server);
 const char* wlg_server_last_error(const wlg_server* server);
+
+/* ---- HDF5 result files without libhdf5 (the prerun/mainrun programs write
+ * the reference's layouts, file_io.cpp:23-192 and utils.cpp:137-236, in
+ * HDF5 superblock-2 files; these read them back).  Paths are '/'-separated
+ * below the root.  Types: 0 uint8, 1 int8, 2 int32, 3 uint64, 4 float64,
+ * 5 compound {Key int32, Value float64} (16 bytes per element). */
+unsigned int wlg_h5_lookup3(const void* data, size_t n, unsigned int init); /* the format's checksum */
+/* Children of a group, one per line, groups with a trailing '/'. */
+wlg_status wlg_h5_list(const char* file, const char* group, char* names, size_t cap);
+/* A dataset's type, element count and (buf != NULL) little-endian bytes. */
+wlg_status wlg_h5_read(const char* file, const char* dataset, int* type, unsigned long long* count, void* buf,
+                       unsigned long long cap_bytes);
+/* A fixed-length string attribute of a dataset (e.g. CodeVersion). */
+wlg_status wlg_h5_attribute(const char* file, const char* dataset, const char* name, char* out, size_t cap);
 
 #ifdef __cplusplus
 }

@@ -50,6 +50,12 @@ SIGNATURES = {
     "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
     "wlg_solve_raw_noalloc": [P, i32, P, P, P, P, i64, P, P],
     "wlg_class_log_probs": [P, P, P, P, i32, f64, P, P],
+    "wlg_prerun": [P, P, i32, P, P, P, P, P],
+    "wlg_mainrun": [P, P, i32, P, P, P, P, P, f64, P, P, P, i64],
+    "wlg_h5_lookup3": [P, sz, u32],
+    "wlg_h5_list": [C.c_char_p, C.c_char_p, P, sz],
+    "wlg_h5_read": [C.c_char_p, C.c_char_p, P, P, P, u64],
+    "wlg_h5_attribute": [C.c_char_p, C.c_char_p, C.c_char_p, P, sz],
     "wlg_server_create": [i32, P, P],
     "wlg_server_submit": [P, P, i32, P],
     "wlg_server_poll": [P, P, i32, P, i32],
@@ -58,6 +64,7 @@ SIGNATURES = {
     "wlg_server_last_error": [P],
 }
 _RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p,
+            "wlg_h5_lookup3": u32,
             "wlg_server_last_error": C.c_char_p}
 
 
@@ -316,3 +323,33 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------ HDF5 files --
+
+H5_TYPES = {0: "u1", 1: "i1", 2: "<i4", 3: "<u8", 4: "<f8", 5: [("Key", "<i4"), ("pad", "<i4"), ("Value", "<f8")]}
+
+
+def h5_list(path: str, group: str = ""):
+    """Children of a group in a result file: (groups, datasets)."""
+    buf = C.create_string_buffer(1 << 20)
+    call("wlg_h5_list", path.encode(), group.encode(), C.cast(buf, P), len(buf))
+    names = buf.value.decode().splitlines()
+    return [n[:-1] for n in names if n.endswith("/")], [n for n in names if not n.endswith("/")]
+
+
+def h5_read(path: str, dataset: str):
+    """A dataset of a result file as a numpy array (compound: fields Key, Value)."""
+    import numpy as np
+    t, n = i32(0), u64(0)
+    call("wlg_h5_read", path.encode(), dataset.encode(), C.byref(t), C.byref(n), None, 0)
+    dt = np.dtype(H5_TYPES[t.value])
+    out = np.zeros(n.value, dt)
+    call("wlg_h5_read", path.encode(), dataset.encode(), C.byref(t), C.byref(n), out.ctypes.data_as(P), out.nbytes)
+    return out
+
+
+def h5_attribute(path: str, dataset: str, name: str) -> str:
+    buf = C.create_string_buffer(4096)
+    call("wlg_h5_attribute", path.encode(), dataset.encode(), name.encode(), C.cast(buf, P), len(buf))
+    return buf.value.decode()

@@ -54,6 +54,7 @@ enum Slot {
   kOut,
   kRes,
   kGpool,
+  kState,
   kSlots
 };
 
@@ -120,9 +121,27 @@ struct Handoff {
   long long n_out = 0;
 };
 
-// Validation, the pre-run of every problem (one launch) and the hand-off to
-// the main run on the host.  Problems that cannot start the main run get
-// their status in `results` and no MainDesc.
+// Pre-run outputs on the host, concatenated in problem order with the
+// offsets of each PreDesc: couplings J8 [2N], visited energies seen [4N+1]
+// (0/1), stored lattices found [n_int][N] (+-1, 0 where none), and fflag
+// [n_int] found flags followed by [n_int] their energies.
+struct PreOut {
+  std::vector<PreDesc> pd;
+  std::vector<int8_t> J8, found;
+  std::vector<uint8_t> seen;
+  std::vector<int> fflag;
+};
+
+// Validation and pre-run descriptors (sizes the PreOut arrays).
+wlg_status prerun_descs(const wlg_problem* probs, int n, wlg_result* results, PreOut& po, int& threads, int& smem,
+                        std::string& err);
+// Validation and the pre-run of every problem (one launch).
+wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, PreOut& po);
+// The hand-off to the main run on the host.  Problems that cannot start the
+// main run get their status in `results` and no MainDesc.
+wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, const PreOut& po, Prepared& prep,
+                   Handoff& ho);
+// run_prerun + handoff.
 wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho);
 
 // Main-run form of a problem by lattice storage: 0 spins in shared memory,

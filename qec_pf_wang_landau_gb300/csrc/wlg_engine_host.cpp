@@ -298,22 +298,21 @@ wlg_status check_problem(const wlg_problem& q)
 
 // Validation, the pre-run of every problem (one launch) and the hand-off to
 // the main run on the host.
-wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho)
+wlg_status prerun_descs(const wlg_problem* probs, int n, wlg_result* results, PreOut& po, int& threads, int& smem,
+                        std::string& err)
 {
-  using clock = std::chrono::steady_clock;
-  ex.h2d = ex.d2h = 0;
-  ex.launches = 0;
-  ex.main_forms = 0;
-  ex.t_pre = ex.t_main = 0;
-  ex.t_handoff = 0;
+  std::vector<PreDesc>& pd = po.pd;
+  pd.assign(static_cast<size_t>(n), PreDesc{});
+  long long oJ = 0, oS = 0, oF = 0, oG = 0;
+  threads = 32;
+  smem = 0;
   for (int p = 0; p < n; ++p) {
-    if (check_problem(probs[p]) != WLG_OK) return fail(ex, WLG_ERR_INVALID, "invalid problem " + std::to_string(p));
+    if (check_problem(probs[p]) != WLG_OK) {
+      err = "invalid problem " + std::to_string(p);
+      return WLG_ERR_INVALID;
+    }
     std::memset(&results[p], 0, sizeof(wlg_result));
   }
-  // ---------------- pre-run
-  std::vector<PreDesc> pd(static_cast<size_t>(n));
-  long long oJ = 0, oS = 0, oF = 0, oG = 0;
-  int threads = 32, smem = 0;
   for (int p = 0; p < n; ++p) {
     const wlg_problem& q = probs[p];
     PreDesc& d = pd[p];
@@ -329,8 +328,10 @@ wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* 
     d.n_int = q.pre_intervals;
     std::vector<int> s, e;
     // prerun.cu:23-25: coarse bins of [-2N, 2N] with overlap 1
-    if (wlg::make_windows(-2 * d.N, 2 * d.N, q.pre_intervals, 1.0F, s, e) != WLG_OK)
-      return fail(ex, WLG_ERR_INVALID, "pre-run intervals produce empty bins");
+    if (wlg::make_windows(-2 * d.N, 2 * d.N, q.pre_intervals, 1.0F, s, e) != WLG_OK) {
+      err = "pre-run intervals produce empty bins";
+      return WLG_ERR_INVALID;
+    }
     d.len_int = e[0] - s[0] + 1;
     d.n_iter = q.pre_iterations;
     d.off_J = oJ;
@@ -346,8 +347,31 @@ wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* 
     threads = std::max(threads, round32(d.walkers));
     results[p].pre_flips = static_cast<long long>(q.pre_walkers) * q.pre_iterations;
   }
-  if (smem > 227 * 1024) return fail(ex, WLG_ERR_INVALID, "pre-run walkers x lattice too large for shared memory");
-  wlg_status st;
+  po.J8.assign(static_cast<size_t>(oJ), 0);
+  po.seen.assign(static_cast<size_t>(oS), 0);
+  po.found.assign(static_cast<size_t>(oF), 0);
+  po.fflag.assign(static_cast<size_t>(oG), 0);
+  if (smem > 227 * 1024) {
+    err = "pre-run walkers x lattice too large for shared memory";
+    return WLG_ERR_INVALID;
+  }
+  return WLG_OK;
+}
+
+wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, PreOut& po)
+{
+  ex.h2d = ex.d2h = 0;
+  ex.launches = 0;
+  ex.main_forms = 0;
+  ex.t_pre = ex.t_main = 0;
+  ex.t_handoff = 0;
+  int threads = 32, smem = 0;
+  std::string err;
+  wlg_status st = prerun_descs(probs, n, results, po, threads, smem, err);
+  if (st != WLG_OK) return fail(ex, st, err);
+  const std::vector<PreDesc>& pd = po.pd;
+  const long long oJ = static_cast<long long>(po.J8.size()), oS = static_cast<long long>(po.seen.size());
+  const long long oF = static_cast<long long>(po.found.size()), oG = static_cast<long long>(po.fflag.size());
   void *d_pd = nullptr, *d_J8 = nullptr, *d_seen = nullptr, *d_found = nullptr, *d_fflag = nullptr;
   if ((st = upload(ex, kPreDesc, pd, &d_pd)) != WLG_OK) return st;
   if ((st = ex.buffer(kJ8, static_cast<size_t>(oJ), &d_J8)) != WLG_OK) return st;
@@ -362,17 +386,26 @@ wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* 
   if (st != WLG_OK) return fail(ex, st, "pre-run launch failed");
   ++ex.launches;
   if (ex.ev != nullptr) cudaEventRecord(ex.ev[1], ex.stream);
-  std::vector<int8_t> J8(static_cast<size_t>(oJ)), found(static_cast<size_t>(oF));
-  std::vector<uint8_t> seen(static_cast<size_t>(oS));
-  std::vector<int> fflag(static_cast<size_t>(oG));
-  download(ex, d_J8, J8);
-  download(ex, d_seen, seen);
-  download(ex, d_found, found);
-  download(ex, d_fflag, fflag);
+  download(ex, d_J8, po.J8);
+  download(ex, d_seen, po.seen);
+  download(ex, d_found, po.found);
+  download(ex, d_fflag, po.fflag);
   if (cudaStreamSynchronize(ex.stream) != cudaSuccess) return fail(ex, WLG_ERR_CUDA, "pre-run failed");
   if (ex.ev != nullptr) cudaEventElapsedTime(&ex.t_pre, ex.ev[0], ex.ev[1]);
+  return WLG_OK;
+}
 
-  // ---------------- hand-off (file_io.cpp:558-659, mainrun.cu:79-113)
+// The hand-off to the main run (file_io.cpp:558-659, mainrun.cu:79-113)
+// from pre-run outputs.
+wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, const PreOut& po, Prepared& prep,
+                   Handoff& ho)
+{
+  using clock = std::chrono::steady_clock;
+  const std::vector<PreDesc>& pd = po.pd;
+  const std::vector<int8_t>& J8 = po.J8;
+  const std::vector<int8_t>& found = po.found;
+  const std::vector<uint8_t>& seen = po.seen;
+  const std::vector<int>& fflag = po.fflag;
   const auto t0 = clock::now();
   std::vector<uint32_t>& Jw = ho.Jw;
   std::vector<uint32_t>& latw = ho.latw;
@@ -529,18 +562,29 @@ wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* 
   return WLG_OK;
 }
 
+wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho)
+{
+  PreOut po;
+  const wlg_status st = run_prerun(ex, probs, n, results, po);
+  if (st != WLG_OK) return st;
+  return handoff(ex, probs, n, results, po, prep, ho);
+}
+
 }  // namespace wlg
 
 namespace {
 
-// The whole batch up to the main-run results.
-wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results,
-                     std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
-                     std::vector<int>& win_host)
+constexpr int kTimedEpoch = 4;  // outer iterations per launch under a time limit
+
+// The main run of a prepared batch: one persistent launch per (form, team
+// size).  time_limit_s > 0: resumable launches of kTimedEpoch outer
+// iterations each, repeated until every problem finished or the limit
+// passed (the reference checks its time limit after each outer iteration,
+// mainrun.cu:376-383); unfinished problems end with WLG_ERR_TIMEOUT.
+wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff& ho, std::vector<MainResult>& mres,
+                    std::vector<double>& out_host, std::vector<int>& win_host, double time_limit_s)
 {
-  Handoff ho;
-  wlg_status st = wlg::prepare_batch(ex, probs, n, results, prep, ho);
-  if (st != WLG_OK) return st;
+  wlg_status st = WLG_OK;
   const std::vector<uint32_t>& Jw = ho.Jw;
   const std::vector<uint32_t>& latw = ho.latw;
   const std::vector<uint32_t>& maskw = ho.maskw;
@@ -596,6 +640,18 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
                           Lmax);
     order.insert(order.end(), idx.begin(), idx.end());
   }
+  const bool timed = time_limit_s > 0;
+  void* d_state = nullptr;
+  if (timed) {  // resumable runs: one state block per problem
+    long long off = 0;
+    for (MainDesc& d : prep.main) {
+      d.off_state = off;
+      d.epoch_outer = kTimedEpoch;
+      off += wlg::align8(wlg::state_layout(d.team, d.I, d.nwL, d.L).bytes);
+    }
+    if ((st = ex.buffer(kState, static_cast<size_t>(off), &d_state)) != WLG_OK) return st;
+    cudaMemsetAsync(d_state, 0, static_cast<size_t>(off), ex.stream);
+  }
   void *d_md = nullptr, *d_order = nullptr, *d_Jw = nullptr, *d_latw = nullptr, *d_win = nullptr, *d_mask = nullptr;
   void *d_out = nullptr, *d_res = nullptr, *d_next = nullptr;
   if ((st = upload(ex, kMainDesc, prep.main, &d_md)) != WLG_OK) return st;
@@ -607,7 +663,7 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
   if ((st = ex.buffer(kOut, static_cast<size_t>(o_out) * sizeof(double), &d_out)) != WLG_OK) return st;
   if ((st = ex.buffer(kRes, static_cast<size_t>(m) * sizeof(MainResult), &d_res)) != WLG_OK) return st;
   if ((st = ex.buffer(kNext, launches.size() * sizeof(int), &d_next)) != WLG_OK) return st;
-  cudaMemsetAsync(d_next, 0, launches.size() * sizeof(int), ex.stream);
+  if (timed) cudaMemsetAsync(d_res, 0, static_cast<size_t>(m) * sizeof(MainResult), ex.stream);
   // grids, and the global log g pool of the variant-3 launches (one slice per
   // resident team, launches side by side)
   std::vector<int> grids(launches.size());
@@ -627,25 +683,48 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
   if (gpool_doubles > 0 &&
       (st = ex.buffer(kGpool, static_cast<size_t>(gpool_doubles) * sizeof(double), &d_gpool)) != WLG_OK)
     return st;
+  auto launch_all = [&]() -> wlg_status {
+    cudaMemsetAsync(d_next, 0, launches.size() * sizeof(int), ex.stream);
+    for (size_t g = 0; g < launches.size(); ++g) {
+      const auto [variant, team, bytes, per_cta, first, count, Lmax] = launches[g];
+      const int grid = grids[g];
+      double* gp = variant == 3 ? static_cast<double*>(d_gpool) + gpool_off[g] : nullptr;
+      const wlg_status s2 = wlg::launch_main_batch(
+        variant, static_cast<const MainDesc*>(d_md), static_cast<const int*>(d_order) + first, count, team, bytes,
+        per_cta, grid, static_cast<int*>(d_next) + g, gp, static_cast<long long>(Lmax) * team,
+        static_cast<const uint32_t*>(d_Jw), static_cast<const uint32_t*>(d_latw), static_cast<const int*>(d_win),
+        static_cast<const uint32_t*>(d_mask), static_cast<double*>(d_out), static_cast<MainResult*>(d_res),
+        static_cast<unsigned char*>(d_state), ex.stream);
+      if (s2 != WLG_OK) return fail(ex, s2, "main-run launch failed");
+      ++ex.launches;
+      ex.main_forms |= 1 << variant;
+    }
+    return WLG_OK;
+  };
   if (ex.ev != nullptr) cudaEventRecord(ex.ev[2], ex.stream);
-  for (size_t g = 0; g < launches.size(); ++g) {
-    const auto [variant, team, bytes, per_cta, first, count, Lmax] = launches[g];
-    const int grid = grids[g];
-    double* gp = variant == 3 ? static_cast<double*>(d_gpool) + gpool_off[g] : nullptr;
-    st = wlg::launch_main_batch(variant, static_cast<const MainDesc*>(d_md), static_cast<const int*>(d_order) + first,
-                                count, team, bytes, per_cta, grid, static_cast<int*>(d_next) + g, gp,
-                                static_cast<long long>(Lmax) * team,
-                                static_cast<const uint32_t*>(d_Jw), static_cast<const uint32_t*>(d_latw),
-                                static_cast<const int*>(d_win), static_cast<const uint32_t*>(d_mask),
-                                static_cast<double*>(d_out), static_cast<MainResult*>(d_res), nullptr, ex.stream);
-    if (st != WLG_OK) return fail(ex, st, "main-run launch failed");
-    ++ex.launches;
-    ex.main_forms |= 1 << variant;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    if ((st = launch_all()) != WLG_OK) return st;
+    if (!timed) break;
+    download(ex, d_res, mres);
+    if (cudaStreamSynchronize(ex.stream) != cudaSuccess) return fail(ex, WLG_ERR_CUDA, "main run failed");
+    bool all = true;
+    for (const MainResult& r : mres) all = all && r.done != 0;
+    if (all) break;
+    if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= time_limit_s) {
+      for (MainResult& r : mres)
+        if (r.done == 0) r.status = WLG_ERR_TIMEOUT;
+      break;
+    }
   }
   if (ex.ev != nullptr) cudaEventRecord(ex.ev[3], ex.stream);
+  std::vector<MainResult> last = mres;
   download(ex, d_res, mres);
   download(ex, d_out, out_host);
   if (cudaStreamSynchronize(ex.stream) != cudaSuccess) return fail(ex, WLG_ERR_CUDA, "main run failed");
+  if (timed)
+    for (int i = 0; i < m; ++i)
+      if (last[i].status == WLG_ERR_TIMEOUT && last[i].done == 0) mres[i].status = WLG_ERR_TIMEOUT;
   if (ex.ev != nullptr) cudaEventElapsedTime(&ex.t_main, ex.ev[2], ex.ev[3]);
   for (int i = 0; i < m; ++i) {
     wlg_result& r = results[prep.main_problem[i]];
@@ -655,6 +734,17 @@ wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* resu
     r.flips = mres[i].flips;
   }
   return WLG_OK;
+}
+
+// The whole batch up to the main-run results.
+wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results,
+                     std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
+                     std::vector<int>& win_host)
+{
+  Handoff ho;
+  const wlg_status st = wlg::prepare_batch(ex, probs, n, results, prep, ho);
+  if (st != WLG_OK) return st;
+  return run_main(ex, results, prep, ho, mres, out_host, win_host, 0.0);
 }
 
 void keep_stats(wlg_context* ctx, const Exec& ex)
@@ -742,6 +832,42 @@ wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, w
 
 namespace {
 
+// Stitched, normalised log g of every problem that finished the main run
+// into caller arrays (wlg_solve layout).
+wlg_status stitch_all(wlg_context* ctx, const Prepared& prep, const std::vector<double>& out,
+                      const std::vector<int>& win, wlg_result* results, int* energies, double* log_g,
+                      long long capacity)
+{
+  const auto t0 = std::chrono::steady_clock::now();
+  long long pos = 0;
+  for (size_t i = 0; i < prep.main.size(); ++i) {
+    const int p = prep.main_problem[i];
+    wlg_result& r = results[p];
+    r.offset = pos;
+    r.n_energies = 0;
+    if (r.status != WLG_OK) continue;
+    const MainDesc& d = prep.main[i];
+    std::vector<std::pair<int, double>> res;
+    const wlg_status sst = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, res);
+    if (sst != WLG_OK) {
+      r.status = sst;
+      continue;
+    }
+    if (pos + static_cast<long long>(res.size()) > capacity) {
+      ctx->err = "result arrays";
+      return WLG_ERR_CAPACITY;
+    }
+    for (size_t k = 0; k < res.size(); ++k) {
+      energies[pos + static_cast<long long>(k)] = res[k].first;
+      log_g[pos + static_cast<long long>(k)] = res[k].second;
+    }
+    r.n_energies = static_cast<int>(res.size());
+    pos += static_cast<long long>(res.size());
+  }
+  ctx->t_stitch = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return WLG_OK;
+}
+
 // The walker-0 log g of every window on the reference's dense layout.
 wlg_status raw_windows(Exec& ex, const wlg_problem* problems, int n, const Prepared& prep,
                        const std::vector<double>& out, const std::vector<int>& win, int* win_start, int* win_end,
@@ -790,34 +916,83 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
   wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
   keep_stats(ctx, ex);
   if (st != WLG_OK) return st;
-  const auto t0 = std::chrono::steady_clock::now();
-  long long pos = 0;
-  for (size_t i = 0; i < prep.main.size(); ++i) {
-    const int p = prep.main_problem[i];
-    wlg_result& r = results[p];
-    r.offset = pos;
-    r.n_energies = 0;
-    if (r.status != WLG_OK) continue;
-    const MainDesc& d = prep.main[i];
-    std::vector<std::pair<int, double>> res;
-    const wlg_status sst = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, res);
-    if (sst != WLG_OK) {
-      r.status = sst;
-      continue;
+  return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+}
+
+wlg_status wlg_prerun(wlg_context* ctx, const wlg_problem* problems, int n, unsigned char* seen,
+                      signed char* couplings, int* found, int* found_energy, signed char* lattices)
+{
+  if (ctx == nullptr || n < 0 || (n > 0 && problems == nullptr)) return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<wlg_result> res(static_cast<size_t>(n));
+  PreOut po;
+  ContextExec ex(ctx);
+  const wlg_status st = run_prerun(ex, problems, n, res.data(), po);
+  keep_stats(ctx, ex);
+  if (st != WLG_OK) return st;
+  long long ob = 0;  // bins so far
+  for (int p = 0; p < n; ++p) {
+    const PreDesc& d = po.pd[p];
+    if (seen != nullptr) std::memcpy(seen + d.off_seen, po.seen.data() + d.off_seen, static_cast<size_t>(4 * d.N + 1));
+    if (couplings != nullptr)
+      std::memcpy(couplings + d.off_J, po.J8.data() + d.off_J, static_cast<size_t>(2 * d.N));
+    if (lattices != nullptr)
+      std::memcpy(lattices + d.off_found, po.found.data() + d.off_found, static_cast<size_t>(d.n_int) * d.N);
+    for (int b = 0; b < d.n_int; ++b) {
+      if (found != nullptr) found[ob + b] = po.fflag[d.off_fflag + b];
+      if (found_energy != nullptr) found_energy[ob + b] = po.fflag[d.off_fflag + d.n_int + b];
     }
-    if (pos + static_cast<long long>(res.size()) > capacity) {
-      ctx->err = "result arrays";
-      return WLG_ERR_CAPACITY;
-    }
-    for (size_t k = 0; k < res.size(); ++k) {
-      energies[pos + static_cast<long long>(k)] = res[k].first;
-      log_g[pos + static_cast<long long>(k)] = res[k].second;
-    }
-    r.n_energies = static_cast<int>(res.size());
-    pos += static_cast<long long>(res.size());
+    ob += d.n_int;
   }
-  ctx->t_stitch = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return WLG_OK;
+}
+
+wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, const unsigned char* seen,
+                       const signed char* couplings, const int* found, const int* found_energy,
+                       const signed char* lattices, double time_limit_s, wlg_result* results, int* energies,
+                       double* log_g, long long capacity)
+{
+  if (ctx == nullptr || n < 0 ||
+      (n > 0 && (problems == nullptr || results == nullptr || seen == nullptr || couplings == nullptr ||
+                 found == nullptr || found_energy == nullptr || lattices == nullptr)))
+    return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ContextExec ex(ctx);
+  ex.h2d = ex.d2h = 0;
+  ex.launches = 0;
+  ex.main_forms = 0;
+  ex.t_pre = ex.t_main = 0;
+  ex.t_handoff = 0;
+  PreOut po;
+  int threads = 0, smem = 0;
+  std::string err;
+  wlg_status st = prerun_descs(problems, n, results, po, threads, smem, err);
+  if (st != WLG_OK) {
+    ctx->err = err;
+    return st;
+  }
+  long long ob = 0;
+  for (int p = 0; p < n; ++p) {
+    const PreDesc& d = po.pd[p];
+    std::memcpy(po.seen.data() + d.off_seen, seen + d.off_seen, static_cast<size_t>(4 * d.N + 1));
+    std::memcpy(po.J8.data() + d.off_J, couplings + d.off_J, static_cast<size_t>(2 * d.N));
+    std::memcpy(po.found.data() + d.off_found, lattices + d.off_found, static_cast<size_t>(d.n_int) * d.N);
+    for (int b = 0; b < d.n_int; ++b) {
+      po.fflag[d.off_fflag + b] = found[ob + b];
+      po.fflag[d.off_fflag + d.n_int + b] = found_energy[ob + b];
+    }
+    ob += d.n_int;
+  }
+  Prepared prep;
+  Handoff ho;
+  std::vector<MainResult> mres;
+  std::vector<double> out;
+  std::vector<int> win;
+  st = handoff(ex, problems, n, results, po, prep, ho);
+  if (st == WLG_OK) st = run_main(ex, results, prep, ho, mres, out, win, time_limit_s);
+  keep_stats(ctx, ex);
+  if (st != WLG_OK) return st;
+  return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
 }
 
 wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)
