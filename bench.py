@@ -222,6 +222,37 @@ def batched_run():
             "main_ms": st["main_ms"], "main_forms": st["main_forms"], "kernel_launches": st["kernel_launches"]}
 
 
+LARGE = dict(sides=(16, 24), samples=38, prob=0.10, seed=4242, max_outer=10)
+
+
+def large_run():
+    """The large-lattice workload (16x16 and 24x24 periodic, p = 0.10, all four
+    classes, 64 windows x 8 walkers, overlap 0.3, exchange every 10, ln f 1e-8),
+    bounded: one wave of 38 samples x 4 classes per side, each capped at 10
+    outer iterations (a run to ln f 1e-8 takes hours).  Reports the WL flip
+    rate and the step time of the 512-thread teams."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = LARGE
+    out = {"workload": "16x16 and 24x24 periodic, p=0.10, classes ivhc, I=64 x W=8, o=0.3, alpha=0.8, ln f 1e-8, "
+                       "exchange every 10; 38 samples x 4 classes per side, capped at 10 outer iterations"}
+    ctx = wlg.Context(0)
+    for L in c["sides"]:
+        N = L * L
+        probs = [wlg.problem(L, L, prob=c["prob"], error_class=cl, seed=c["seed"], sample=k, pre_walkers=128,
+                             pre_intervals=128, pre_iterations=100 * N, intervals=64, walkers_per_interval=8,
+                             overlap=0.3, alpha=0.8, beta=1e-8, iterations=1000, exchange_every=10,
+                             max_outer=c["max_outer"]) for k in range(c["samples"]) for cl in "ivhc"]
+        res = ctx.solve_raw(probs)
+        st = ctx.stats()
+        flips = sum(r.flips for r, _, _, _ in res)
+        outer = max(r.outer_iterations for r, _, _, _ in res)
+        out[f"{L}x{L}"] = {"problems": len(probs), "flips_per_s": flips / (st["main_ms"] / 1e3),
+                           "main_ms": st["main_ms"], "pre_ms": st["pre_ms"],
+                           "us_per_step": st["main_ms"] * 1e3 / (outer * 1000), "main_forms": st["main_forms"],
+                           "ran": sum(1 for r, _, _, _ in res if r.status in (0, 7))}
+    return out
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -397,6 +428,7 @@ def run_ours(args):
         line["clocks"] = clocks
     if not args.no_extra:
         line["batched"] = batched_run()
+        line["large"] = large_run()
         line["serving"] = serving_run()
     return line
 
@@ -467,7 +499,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--profile-case", default=None, help="run a small fixed case for a profiler and exit")
-    ap.add_argument("--leg", default=None, choices=["serving", "batched"], help="run one extra leg alone and print it")
+    ap.add_argument("--leg", default=None, choices=["serving", "batched", "large"],
+                    help="run one extra leg alone and print it")
     ap.add_argument("--no-extra", action="store_true", help="skip the serving and batched legs")
     args = ap.parse_args()
     if args.profile_case:
@@ -476,7 +509,8 @@ def main():
     if args.leg is not None:
         import qec_pf_wang_landau_gb300 as wlg
         wlg.build()
-        print(json.dumps({args.leg: serving_run() if args.leg == "serving" else batched_run()}), flush=True)
+        legs = {"serving": serving_run, "batched": batched_run, "large": large_run}
+        print(json.dumps({args.leg: legs[args.leg]()}), flush=True)
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:

@@ -139,6 +139,32 @@ def test_engine_global_log_g_form_bit_exact(cuda, cfg):
         assert np.array_equal(wins[b], want), f"window {b}: max |d| {np.abs(wins[b] - want).max()}"
 
 
+# Large lattices with the large-lattice workload's window layout: 64 windows
+# x 8 walkers (512-thread teams), overlap 0.3, exchange every 10 iterations,
+# p = 0.10; capped at two outer iterations.  24x24 runs in the global-pool
+# form, 16x16 in shared memory.
+LARGE = [
+    (24, 24, 0, 0.10, "h", 4242, 1, 128, 128, 57600, 64, 8, 0.3, 0.8, 1e-8, 1000, 10, 1, 0),
+    (16, 16, 0, 0.10, "c", 4242, 1, 128, 128, 25600, 64, 8, 0.3, 0.8, 1e-8, 1000, 10, 1, 0),
+]
+
+
+@pytest.mark.parametrize("cfg", LARGE, ids=[f"{c[0]}x{c[1]}I{c[10]}W{c[11]}" for c in LARGE])
+def test_engine_large_teams_bit_exact(cuda, cfg):
+    import qec_pf_wang_landau_gb300 as wlg
+    I, W = cfg[10], cfg[11]
+    ref = oracle_run(*cfg, max_outer=2)
+    assert ref["status"] == 3
+    ctx = wlg.Context(0)
+    (res, s, e, wins), = ctx.solve_raw(big_problems(cfg, max_outer=2))
+    assert res.status == wlg.WLG_ERR_TIMEOUT and res.flips == ref["flips"]
+    assert np.array_equal(s, ref["start"][:I]) and np.array_equal(e, ref["end"][:I])
+    for b in range(I):
+        o = ref["off_hist"][b * W]
+        want = ref["logG"][o:o + (e[b] - s[b] + 1)]
+        assert np.array_equal(wins[b], want), f"window {b}: max |d| {np.abs(wins[b] - want).max()}"
+
+
 def test_engine_mixed_forms_batch_equals_separate_runs(cuda):
     """A batch holding shared-memory-form and global-pool-form problems (two
     persistent launches, one global pool) gives each problem its result alone."""
