@@ -274,6 +274,25 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
 wlg_status wlg_solve_plain(const wlg_problem* problems, int n, wlg_result* results, int* energies, double* log_g,
                            long long capacity, wlg_stream stream, long long* kernel_launches);
 
+/* Autotuner: teams (problems) per CTA of the main-run launches, i.e. walkers
+ * and windows per block.  The batch is prepared once and its main run timed
+ * (CUDA events) with every power-of-two teams-per-CTA up to 256 threads per
+ * CTA, each problem capped at max_outer outer iterations; the fastest choice
+ * per (main-run form, team size) is kept by the context and used by every
+ * later solve on it.  Results never depend on the choice (each problem's
+ * trajectory is its own).  out[i] (up to cap) describes group i; *n_out =
+ * number of groups. */
+typedef struct {
+  int form;        /* main-run form: 0 shared-memory lattice, 1 register lattice, 2 register + table */
+  int team;        /* threads per team (walkers, rounded up to a warp) */
+  int per_cta;     /* chosen teams per CTA */
+  float main_ms;   /* its main-run time on the capped batch */
+  int candidates;  /* choices timed */
+} wlg_tuning;
+
+wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, int n, int max_outer,
+                                wlg_tuning* out, int cap, int* n_out);
+
 /* What the last wlg_solve / wlg_solve_raw did: time by phase in
  * milliseconds (device phases by CUDA events on the context's stream, host
  * phases by the host clock), bytes copied host->device and device->host,

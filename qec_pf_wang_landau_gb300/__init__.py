@@ -56,6 +56,7 @@ SIGNATURES = {
     "wlg_h5_list": [C.c_char_p, C.c_char_p, P, sz],
     "wlg_h5_read": [C.c_char_p, C.c_char_p, P, P, P, u64],
     "wlg_h5_attribute": [C.c_char_p, C.c_char_p, C.c_char_p, P, sz],
+    "wlg_context_autotune": [P, P, i32, i32, P, i32, P],
     "wlg_server_create": [i32, P, P],
     "wlg_server_submit": [P, P, i32, P],
     "wlg_server_poll": [P, P, i32, P, i32],
@@ -199,11 +200,26 @@ class Context:
             out.append((res[p], s, e, wins))
         return out
 
+    def autotune(self, problems, max_outer: int = 2):
+        """Time teams-per-CTA choices on `problems` (capped at max_outer outer
+        iterations) and keep the fastest per (form, team size) for later solves."""
+        n = len(problems)
+        arr = (Problem * n)(*problems)
+        out = (Tuning * 16)()
+        k = i32(0)
+        self._check("wlg_context_autotune", lib().wlg_context_autotune(self._h, C.cast(arr, P), n, max_outer,
+                                                                        C.cast(out, P), 16, C.byref(k)))
+        return [{f: getattr(out[i], f) for f, _ in Tuning._fields_} for i in range(min(k.value, 16))]
+
     def stats(self):
         """What the last solve did: ms by phase, bytes copied each way, kernels launched."""
         st = Stats()
         call("wlg_last_stats", self._h, C.byref(st))
         return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("form", i32), ("team", i32), ("per_cta", i32), ("main_ms", f32), ("candidates", i32)]
 
 
 class Stats(C.Structure):

@@ -70,6 +70,9 @@ struct Exec {
   int launches = 0;
   int main_forms = 0;  // bit v: a main-run launch of form v
   std::string err;
+  // teams per CTA chosen by an autotuner, by (form, team size); nullptr or
+  // no entry: the built-in rule
+  const std::map<std::pair<int, int>, int>* per_cta = nullptr;
   virtual ~Exec() = default;
   // device buffer for `slot` of at least `bytes` bytes
   virtual wlg_status buffer(Slot slot, size_t bytes, void** out) = 0;

@@ -232,6 +232,7 @@ struct wlg_context {
   long long h2d = 0, d2h = 0;
   int launches = 0;
   int main_forms = 0;
+  std::map<std::pair<int, int>, int> tuned;  // teams per CTA by (form, team size), from wlg_context_autotune
   std::string err;
 };
 
@@ -269,6 +270,7 @@ struct ContextExec final : Exec {
     device = c->device;
     stream = c->stream;
     ev = c->ev;
+    per_cta = &c->tuned;
   }
   wlg_status buffer(Slot slot, size_t bytes, void** out) override
   {
@@ -636,6 +638,13 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
     // than packing them into few CTAs
     per_cta = std::min(per_cta, static_cast<int>(idx.size()) / (2 * sms));
     per_cta = std::max(per_cta, 1);
+    if (ex.per_cta != nullptr) {
+      auto it = ex.per_cta->find({variant, team});
+      if (it != ex.per_cta->end()) {
+        per_cta = std::max(1, std::min(it->second, team <= 256 ? 256 / team : 1));
+        per_cta = std::max(1, std::min(per_cta, (227 * 1024) / bytes));
+      }
+    }
     launches.emplace_back(variant, team, bytes, per_cta, static_cast<int>(order.size()), static_cast<int>(idx.size()),
                           Lmax);
     order.insert(order.end(), idx.begin(), idx.end());
@@ -993,6 +1002,75 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
   keep_stats(ctx, ex);
   if (st != WLG_OK) return st;
   return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+}
+
+wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, int n, int max_outer,
+                                wlg_tuning* out, int cap, int* n_out)
+{
+  if (ctx == nullptr || n <= 0 || problems == nullptr || max_outer <= 0 || (cap > 0 && out == nullptr))
+    return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<wlg_problem> probs(problems, problems + n);
+  for (wlg_problem& q : probs) q.max_outer = max_outer;
+  std::vector<wlg_result> res(static_cast<size_t>(n));
+  ContextExec ex(ctx);
+  Prepared prep;
+  Handoff ho;
+  wlg_status st = wlg::prepare_batch(ex, probs.data(), n, res.data(), prep, ho);
+  if (st != WLG_OK) {
+    ctx->err = ex.err;
+    return st;
+  }
+  // problems by (form, team size), as run_main groups them
+  std::map<std::pair<int, int>, std::vector<int>> groups;
+  for (size_t i = 0; i < prep.main.size(); ++i) {
+    const MainDesc& d = prep.main[i];
+    int form = main_form(d);
+    if (form == 0 && team_bytes(d, 0, d.team) > 227 * 1024) form = 3;
+    groups[{form == 3 ? 0 : form, d.team}].push_back(static_cast<int>(i));
+  }
+  std::map<std::pair<int, int>, int> best;
+  std::vector<wlg_tuning> found;
+  for (const auto& [key, idx] : groups) {
+    Prepared sub;
+    for (int i : idx) {
+      sub.main.push_back(prep.main[i]);
+      sub.main_problem.push_back(prep.main_problem[i]);
+    }
+    const int limit = key.second <= 256 ? 256 / key.second : 1;
+    wlg_tuning t{key.first, key.second, 1, 0.0f, 0};
+    float best_ms = 0.0f;
+    for (int c = 1; c <= limit; c *= 2) {
+      std::map<std::pair<int, int>, int> force{{key, c}};
+      // the form recorded for the launch may be 3 when the team's state does
+      // not fit shared memory; force both keys
+      force[{3, key.second}] = c;
+      ex.per_cta = &force;
+      std::vector<MainResult> mres;
+      std::vector<double> out_host;
+      std::vector<int> win_host;
+      Prepared run = sub;
+      st = run_main(ex, res.data(), run, ho, mres, out_host, win_host, 0.0);
+      if (st != WLG_OK) {
+        ctx->err = ex.err;
+        return st;
+      }
+      if (c == 1 || ex.t_main < best_ms) {
+        best_ms = ex.t_main;
+        t.per_cta = c;
+      }
+      ++t.candidates;
+    }
+    t.main_ms = best_ms;
+    best[key] = t.per_cta;
+    best[{3, key.second}] = t.per_cta;
+    found.push_back(t);
+  }
+  for (const auto& [k, v] : best) ctx->tuned[k] = v;
+  const int k = std::min(cap, static_cast<int>(found.size()));
+  for (int i = 0; i < k; ++i) out[i] = found[i];
+  if (n_out != nullptr) *n_out = static_cast<int>(found.size());
+  return WLG_OK;
 }
 
 wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)

@@ -197,6 +197,24 @@ def test_engine_heterogeneous_batch_equals_separate_runs(cuda):
         assert np.array_equal(E, E1) and np.array_equal(G, G1)
 
 
+def test_autotune_picks_teams_per_cta_without_changing_results(cuda):
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = [wlg.problem(6, 6, prob=0.04, error_class=c, seed=99, sample=k, beta=0.01, iterations=500)
+             for k in range(12) for c in "ivhc"] + \
+            [wlg.problem(9, 9, prob=0.05, error_class="i", seed=99, sample=k, intervals=8, walkers_per_interval=6,
+                         beta=0.05, iterations=400) for k in range(4)]
+    ctx = wlg.Context(0)
+    before = ctx.solve(probs)
+    tuned = ctx.autotune(probs, max_outer=2)
+    assert len(tuned) == 2  # (form 2, 32 threads) and (form 0, 64 threads)
+    for t in tuned:
+        assert t["candidates"] >= 1 and 1 <= t["per_cta"] <= 256 // t["team"] and t["main_ms"] > 0
+    after = ctx.solve(probs)
+    for (r1, E1, G1), (r2, E2, G2) in zip(before, after):
+        assert r1.status == r2.status and r1.outer_iterations == r2.outer_iterations
+        assert np.array_equal(E1, E2) and np.array_equal(G1, G2)
+
+
 def test_engine_4x4_log_g_against_exact_enumeration(cuda):
     """Config 1 (4x4 periodic, p=0.04, seed 12345, class i): the normalised log g
     against exact FP64 enumeration of all 2^16 states."""
