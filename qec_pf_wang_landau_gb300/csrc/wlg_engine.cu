@@ -477,6 +477,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       bool stopped = false;
       int ovr_site = -1;  // exact site of the step being replayed
       int ovr_acc = -1;   // exact acceptance of the step being replayed
+      int q = static_cast<int>(pos - (blk << 2));  // draw offset in block A, 0..3
+      uint64_t nc = blk + 2;                        // counter of the block being built in C
       for (;;) {
         const bool act = it < d.n_iter && !stopped;
         if (!__any_sync(wmask, act)) break;
@@ -485,7 +487,6 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
           Cb = phase < 2 ? half : Cb;
           phase = min(phase + 1, 2);
         }
-        const int q = static_cast<int>(pos - (blk << 2));
         const uint32_t x1 = pick_word(A, B, q);
         const uint32_t x2 = pick_word(A, B, q + 1);
         const float lu = log_uniform(x2);  // depends on the draw only: off the serial path
@@ -523,7 +524,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         // sequential double additions in g_cur and the double differences,
         // each <= one rounding at |g| (k + 4 ulp_g); the shadows' absolute
         // error 2^-44 (g + gbase) each (<= 512 ulp_g for both)
-        const float eps = 0x1p-22f * (fabsf(gfb) + fabsf(gfn) + kl + fabsf(df)) + (kf + 516.0f) * ulp_g;
+        const float eps_b = fmaf(0x1p-22f, fabsf(gfb) + kl, (kf + 516.0f) * ulp_g);  // before the load of gfn
+        const float eps = fmaf(0x1p-22f, fabsf(gfn) + fabsf(df), eps_b);
         const Decision dec = decide(x2, lu, df, eps, same);
         const bool fast_acc = dec.acc;
         const bool known = dec.known;
@@ -560,16 +562,18 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         owed = upd ? lnf : 0.0;
         h_cur += upd ? 1u : 0u;
         kf += upd ? 1.0f : 0.0f;
-        pos += commit ? (inside ? 2 : 1) : (stop_now ? 1 : 0);
+        const int used = commit ? (inside ? 2 : 1) : (stop_now ? 1 : 0);  // draws consumed
+        pos += static_cast<uint64_t>(used);
+        q += used;
         it += commit ? 1 : 0;
         stopped = stopped || stop_now;
         ovr_site = commit || stop_now ? -1 : ovr_site;
         ovr_acc = commit || stop_now ? -1 : ovr_acc;
-        const bool adv = (pos >> 2) != blk;
+        const bool adv = q >= 4;
+        q = adv ? q - 4 : q;
         A = adv ? B : A;
         B = adv ? Cb : B;
-        blk = adv ? blk + 1 : blk;
-        const uint64_t nc = blk + 2;  // restart C on the counter after the new B
+        nc += adv ? 1u : 0u;  // restart C on the counter after the new B
         Cb = adv ? make_uint4(static_cast<uint32_t>(nc), static_cast<uint32_t>(nc >> 32), rng.s0, rng.s1) : Cb;
         phase = adv ? 0 : phase;
         if (__any_sync(wmask, need_site || need_acc)) {  // rare
