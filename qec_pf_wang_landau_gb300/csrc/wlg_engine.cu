@@ -106,17 +106,41 @@ __global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ 
   int energy = misc[0];
   if (live) rng.init(key_u32(d.seed, static_cast<uint64_t>(d.sample)), 2 + static_cast<uint64_t>(w), 0);
   const double site_scale = (N - 1 + 0.999999);
+  const uint32_t site_thr = static_cast<uint32_t>(N) * 2048u + 16384u;  // as MainDesc::site_thr
+  // u < exp(H[old] - H[new]) (wl.cu:536-537) for an integer count difference
+  // dd: always for dd >= 1 (exp(dd) > 1 >= u); never for dd <= -25
+  // (exp(dd) < 2^-33 <= u); else x < acc_thr[-dd], the least draw whose
+  // uniform reaches the device's exp(dd) (uniforms are monotone in the draw)
+  __shared__ uint32_t acc_thr[25];
+  if (tid < 25) {
+    const double e = exp(static_cast<double>(-tid));
+    unsigned long long lo = 0, hi = 1ull << 32;
+    while (lo < hi) {
+      const unsigned long long mid = (lo + hi) >> 1;
+      if (static_cast<double>(unit_float(static_cast<uint32_t>(mid))) >= e) hi = mid;
+      else lo = mid + 1;
+    }
+    acc_thr[tid] = static_cast<uint32_t>(lo);  // <= 2^32 - 128: u reaches 1 there
+  }
+  __syncthreads();
   bool ok = live;
   for (int it = 0; it < d.n_iter; ++it) {
     int hit = -1;
     bool acc = false;
     if (ok) {
-      const Move m = propose_i8(rng, s, J, energy, X, Y, site_scale, d.boundary);
+      // site trunc(u (N - 1 + 0.999999)) (wl.cu:60-66): floor(x N / 2^32)
+      // unless x N lies next to a multiple of 2^32 (see the main run)
+      const uint32_t xs = rng.raw();
+      const uint32_t lo_s = xs * static_cast<uint32_t>(N);
+      int site = static_cast<int>(__umulhi(xs, static_cast<uint32_t>(N)));
+      if (lo_s < site_thr || lo_s > ~site_thr)
+        site = static_cast<int>(trunc(static_cast<double>(unit_float(xs)) * site_scale));
+      const Move m = move_i8(s, J, energy, X, Y, site, d.boundary);
       const int io = energy - e_min;
       const int in = m.new_energy - e_min;
-      const double prob = exp(static_cast<double>(hist[io]) - static_cast<double>(hist[in]));
-      const double u = rng.uniform();
-      if (u < prob) {
+      const long long dd = static_cast<long long>(hist[io]) - static_cast<long long>(hist[in]);
+      const uint32_t xa = rng.raw();
+      if (dd >= 1 || (dd >= -24 && xa < acc_thr[-dd])) {
         s[m.site] = static_cast<int8_t>(-s[m.site]);
         energy = m.new_energy;
         acc = true;

@@ -14,6 +14,7 @@
 #include <map>
 #include <numbers>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -848,20 +849,38 @@ wlg_status stitch_all(wlg_context* ctx, const Prepared& prep, const std::vector<
                       long long capacity)
 {
   const auto t0 = std::chrono::steady_clock::now();
+  const size_t m = prep.main.size();
+  // problems are independent: stitch them on the host's cores, then pack in
+  // problem order
+  std::vector<std::vector<std::pair<int, double>>> curves(m);
+  std::vector<wlg_status> sst(m, WLG_OK);
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t workers = std::min<size_t>({static_cast<size_t>(hw), 16, (m + 31) / 32});
+  auto work = [&](size_t w) {
+    for (size_t i = w; i < m; i += workers) {
+      if (results[prep.main_problem[i]].status != WLG_OK) continue;
+      const MainDesc& d = prep.main[i];
+      sst[i] = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, curves[i]);
+    }
+  };
+  if (workers <= 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (size_t w = 0; w < workers; ++w) pool.emplace_back(work, w);
+    for (std::thread& th : pool) th.join();
+  }
   long long pos = 0;
-  for (size_t i = 0; i < prep.main.size(); ++i) {
-    const int p = prep.main_problem[i];
-    wlg_result& r = results[p];
+  for (size_t i = 0; i < m; ++i) {
+    wlg_result& r = results[prep.main_problem[i]];
     r.offset = pos;
     r.n_energies = 0;
     if (r.status != WLG_OK) continue;
-    const MainDesc& d = prep.main[i];
-    std::vector<std::pair<int, double>> res;
-    const wlg_status sst = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, res);
-    if (sst != WLG_OK) {
-      r.status = sst;
+    if (sst[i] != WLG_OK) {
+      r.status = sst[i];
       continue;
     }
+    const auto& res = curves[i];
     if (pos + static_cast<long long>(res.size()) > capacity) {
       ctx->err = "result arrays";
       return WLG_ERR_CAPACITY;

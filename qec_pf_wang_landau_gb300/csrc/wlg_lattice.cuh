@@ -17,13 +17,11 @@ struct Move {
 // reference), dE from the four neighbours; open boundaries drop the bonds
 // that would wrap.  Couplings: right bond of (i,j) at i*Y+j, down bond at
 // N+i*Y+j.
-__device__ __forceinline__ Move propose_i8(Stream& rng, const int8_t* __restrict__ s, const int8_t* __restrict__ J,
-                                           int E, int X, int Y, double site_scale, int boundary)
+// Energy after flipping `site` of the int8 lattice s (wl.cu:52-156).
+__device__ __forceinline__ Move move_i8(const int8_t* __restrict__ s, const int8_t* __restrict__ J, int E, int X,
+                                        int Y, int site, int boundary)
 {
   const int N = X * Y;
-  double u = rng.uniform();
-  u *= site_scale;
-  const int site = static_cast<int>(trunc(u));
   const int i = site / Y;
   const int j = site - i * Y;
   const int ip = (i + 1 < X) ? i + 1 : 0;
@@ -42,6 +40,15 @@ __device__ __forceinline__ Move propose_i8(Stream& rng, const int8_t* __restrict
   }
   const int dE = -2 * s[site] * (up + left + down + right);
   return {E - dE, site};
+}
+
+// A uniform site and its flipped energy (wl.cu:60-66 then :52-156).
+__device__ __forceinline__ Move propose_i8(Stream& rng, const int8_t* __restrict__ s, const int8_t* __restrict__ J,
+                                           int E, int X, int Y, double site_scale, int boundary)
+{
+  double u = rng.uniform();
+  u *= site_scale;
+  return move_i8(s, J, E, X, Y, static_cast<int>(trunc(u)), boundary);
 }
 
 // wl.cu:261-340.
