@@ -181,6 +181,44 @@ def test_engine_mixed_forms_batch_equals_separate_runs(cuda):
         assert all(np.array_equal(a, b) for a, b in zip(wins, wins1))
 
 
+def random_configs(n, seed=20261203):
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        X, Y = int(rng.integers(3, 10)), int(rng.integers(3, 10))
+        I = int(rng.integers(2, 9))
+        out.append((X, Y, int(rng.integers(0, 2)), float(np.float32(rng.uniform(0.02, 0.2))), "ivhc"[rng.integers(0, 4)],
+                    int(rng.integers(1, 10 ** 6)), 1, 64, 16, 2000, I, int(rng.integers(1, 6)),
+                    float(rng.choice([0.2, 0.25, 0.5])), 0.8, 0.02, int(rng.integers(200, 1001)),
+                    int(rng.choice([1, 2, 5, 20])), int(rng.integers(0, 2)), int(rng.integers(0, 2))))
+    return out
+
+
+def test_engine_random_configs_bit_exact_in_one_batch(cuda):
+    """Seeded random problems (size, boundary, class, p, windows, walkers,
+    overlap, n, exchange cadence, mode and parity) in one heterogeneous batch:
+    each equals the oracle's run of it alone, capped at 6 outer iterations."""
+    import qec_pf_wang_landau_gb300 as wlg
+    cfgs = random_configs(12)
+    refs = [oracle_run(*c, max_outer=6) for c in cfgs]
+    probs = [big_problems(c, max_outer=6)[0] for c in cfgs]
+    out = wlg.Context(0).solve_raw(probs)
+    compared = 0
+    for c, ref, (res, s, e, wins) in zip(cfgs, refs, out):
+        I, W = c[10], c[11]
+        if ref["status"] not in (0, 3):
+            assert res.status != 0, c  # the oracle's run stopped on a new energy or had no lattice
+            continue
+        assert res.status == (0 if ref["status"] == 0 else wlg.WLG_ERR_TIMEOUT), c
+        assert res.flips == ref["flips"], c
+        assert np.array_equal(s, ref["start"][:I]) and np.array_equal(e, ref["end"][:I]), c
+        for b in range(I):
+            o = ref["off_hist"][b * W]
+            assert np.array_equal(wins[b], ref["logG"][o:o + (e[b] - s[b] + 1)]), (c, b)
+        compared += 1
+    assert compared >= 8
+
+
 def test_engine_heterogeneous_batch_equals_separate_runs(cuda):
     """Problems of different shapes in one batch give the same results as alone."""
     import qec_pf_wang_landau_gb300 as wlg
