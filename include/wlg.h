@@ -203,6 +203,10 @@ typedef struct wlg_context wlg_context;
 wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context** out);
 wlg_status wlg_context_destroy(wlg_context* ctx);
 const char* wlg_context_last_error(const wlg_context* ctx);
+/* Later solves on ctx run on `stream` (NULL: the context's own stream);
+ * work already queued on the previous stream is finished first.  Solves
+ * still return after their stream has reached the results. */
+wlg_status wlg_context_set_stream(wlg_context* ctx, wlg_stream stream);
 
 /* Runs pre-run and main run of n problems as one batch on the GPU and
  * returns each problem's stitched, normalised log g (result_handling.cpp,

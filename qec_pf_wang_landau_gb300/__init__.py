@@ -44,6 +44,7 @@ SIGNATURES = {
     "wlg_context_create": [i32, sz, P],
     "wlg_context_destroy": [P],
     "wlg_context_last_error": [P],
+    "wlg_context_set_stream": [P, P],
     "wlg_solve": [P, P, i32, P, P, P, i64],
     "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
     "wlg_last_stats": [P, P],
@@ -199,6 +200,12 @@ class Context:
                     pos += ln
             out.append((res[p], s, e, wins))
         return out
+
+    def set_stream(self, stream=None):
+        """Run later solves on a CUDA stream handle (int, e.g. torch's
+        Stream.cuda_stream); None: the context's own stream."""
+        self._check("wlg_context_set_stream",
+                    lib().wlg_context_set_stream(self._h, C.c_void_p(stream) if stream else None))
 
     def autotune(self, problems, max_outer: int = 2):
         """Time teams-per-CTA choices on `problems` (capped at max_outer outer

@@ -223,7 +223,8 @@ struct DevBuf {
 
 struct wlg_context {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // where solves run
+  cudaStream_t own_stream = nullptr;  // the context's own stream
   size_t budget = 0;
   size_t used = 0;
   DevBuf buf[kSlots];
@@ -790,21 +791,24 @@ extern "C" {
 
 wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context** out)
 {
-  if (out == nullptr) return WLG_ERR_INVALID;
-  *out = nullptr;
-  int n = 0;
-  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return WLG_ERR_INVALID;
-  if (cudaSetDevice(device) != cudaSuccess) return WLG_ERR_CUDA;
-  auto* ctx = new wlg_context();
-  ctx->device = device;
-  ctx->budget = mem_budget_bytes;
-  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    delete ctx;
-    return WLG_ERR_CUDA;
-  }
-  for (auto& e : ctx->ev) cudaEventCreate(&e);
-  *out = ctx;
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (out == nullptr) return WLG_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return WLG_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return WLG_ERR_CUDA;
+    auto* ctx = new wlg_context();
+    ctx->device = device;
+    ctx->budget = mem_budget_bytes;
+    if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return WLG_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    for (auto& e : ctx->ev) cudaEventCreate(&e);
+    *out = ctx;
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_context_destroy(wlg_context* ctx)
@@ -815,8 +819,17 @@ wlg_status wlg_context_destroy(wlg_context* ctx)
   for (DevBuf& b : ctx->buf)
     if (b.p != nullptr) cudaFree(b.p);
   for (auto& e : ctx->ev) cudaEventDestroy(e);
-  cudaStreamDestroy(ctx->stream);
+  cudaStreamDestroy(ctx->own_stream);
   delete ctx;
+  return WLG_OK;
+}
+
+wlg_status wlg_context_set_stream(wlg_context* ctx, wlg_stream stream)
+{
+  if (ctx == nullptr) return WLG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return WLG_ERR_CUDA;
+  ctx->stream = stream != nullptr ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
   return WLG_OK;
 }
 
@@ -825,17 +838,19 @@ const char* wlg_context_last_error(const wlg_context* ctx) { return ctx == nullp
 wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* win_start,
                          int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset)
 {
-  if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  std::vector<MainResult> mres;
-  Prepared prep;
-  std::vector<double> out;
-  std::vector<int> win;
-  ContextExec ex(ctx);
-  wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
-  keep_stats(ctx, ex);
-  if (st != WLG_OK) return st;
-  return raw_windows(ex, problems, n, prep, out, win, win_start, win_end, raw_log_g, raw_capacity, raw_offset);
+  return wlg::guarded([&]() -> wlg_status {
+    if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<MainResult> mres;
+    Prepared prep;
+    std::vector<double> out;
+    std::vector<int> win;
+    ContextExec ex(ctx);
+    wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
+    keep_stats(ctx, ex);
+    if (st != WLG_OK) return st;
+    return raw_windows(ex, problems, n, prep, out, win, win_start, win_end, raw_log_g, raw_capacity, raw_offset);
+  });
 }
 
 }  // extern "C"
@@ -934,45 +949,49 @@ extern "C" {
 wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* energies,
                      double* log_g, long long capacity)
 {
-  if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  std::vector<MainResult> mres;
-  Prepared prep;
-  std::vector<double> out;
-  std::vector<int> win;
-  ContextExec ex(ctx);
-  wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
-  keep_stats(ctx, ex);
-  if (st != WLG_OK) return st;
-  return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+  return wlg::guarded([&]() -> wlg_status {
+    if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<MainResult> mres;
+    Prepared prep;
+    std::vector<double> out;
+    std::vector<int> win;
+    ContextExec ex(ctx);
+    wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
+    keep_stats(ctx, ex);
+    if (st != WLG_OK) return st;
+    return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+  });
 }
 
 wlg_status wlg_prerun(wlg_context* ctx, const wlg_problem* problems, int n, unsigned char* seen,
                       signed char* couplings, int* found, int* found_energy, signed char* lattices)
 {
-  if (ctx == nullptr || n < 0 || (n > 0 && problems == nullptr)) return WLG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  std::vector<wlg_result> res(static_cast<size_t>(n));
-  PreOut po;
-  ContextExec ex(ctx);
-  const wlg_status st = run_prerun(ex, problems, n, res.data(), po);
-  keep_stats(ctx, ex);
-  if (st != WLG_OK) return st;
-  long long ob = 0;  // bins so far
-  for (int p = 0; p < n; ++p) {
-    const PreDesc& d = po.pd[p];
-    if (seen != nullptr) std::memcpy(seen + d.off_seen, po.seen.data() + d.off_seen, static_cast<size_t>(4 * d.N + 1));
-    if (couplings != nullptr)
-      std::memcpy(couplings + d.off_J, po.J8.data() + d.off_J, static_cast<size_t>(2 * d.N));
-    if (lattices != nullptr)
-      std::memcpy(lattices + d.off_found, po.found.data() + d.off_found, static_cast<size_t>(d.n_int) * d.N);
-    for (int b = 0; b < d.n_int; ++b) {
-      if (found != nullptr) found[ob + b] = po.fflag[d.off_fflag + b];
-      if (found_energy != nullptr) found_energy[ob + b] = po.fflag[d.off_fflag + d.n_int + b];
+  return wlg::guarded([&]() -> wlg_status {
+    if (ctx == nullptr || n < 0 || (n > 0 && problems == nullptr)) return WLG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<wlg_result> res(static_cast<size_t>(n));
+    PreOut po;
+    ContextExec ex(ctx);
+    const wlg_status st = run_prerun(ex, problems, n, res.data(), po);
+    keep_stats(ctx, ex);
+    if (st != WLG_OK) return st;
+    long long ob = 0;  // bins so far
+    for (int p = 0; p < n; ++p) {
+      const PreDesc& d = po.pd[p];
+      if (seen != nullptr) std::memcpy(seen + d.off_seen, po.seen.data() + d.off_seen, static_cast<size_t>(4 * d.N + 1));
+      if (couplings != nullptr)
+        std::memcpy(couplings + d.off_J, po.J8.data() + d.off_J, static_cast<size_t>(2 * d.N));
+      if (lattices != nullptr)
+        std::memcpy(lattices + d.off_found, po.found.data() + d.off_found, static_cast<size_t>(d.n_int) * d.N);
+      for (int b = 0; b < d.n_int; ++b) {
+        if (found != nullptr) found[ob + b] = po.fflag[d.off_fflag + b];
+        if (found_energy != nullptr) found_energy[ob + b] = po.fflag[d.off_fflag + d.n_int + b];
+      }
+      ob += d.n_int;
     }
-    ob += d.n_int;
-  }
-  return WLG_OK;
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, const unsigned char* seen,
@@ -980,116 +999,120 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
                        const signed char* lattices, double time_limit_s, wlg_result* results, int* energies,
                        double* log_g, long long capacity)
 {
-  if (ctx == nullptr || n < 0 ||
-      (n > 0 && (problems == nullptr || results == nullptr || seen == nullptr || couplings == nullptr ||
-                 found == nullptr || found_energy == nullptr || lattices == nullptr)))
-    return WLG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  ContextExec ex(ctx);
-  ex.h2d = ex.d2h = 0;
-  ex.launches = 0;
-  ex.main_forms = 0;
-  ex.t_pre = ex.t_main = 0;
-  ex.t_handoff = 0;
-  PreOut po;
-  int threads = 0, smem = 0;
-  std::string err;
-  wlg_status st = prerun_descs(problems, n, results, po, threads, smem, err);
-  if (st != WLG_OK) {
-    ctx->err = err;
-    return st;
-  }
-  long long ob = 0;
-  for (int p = 0; p < n; ++p) {
-    const PreDesc& d = po.pd[p];
-    std::memcpy(po.seen.data() + d.off_seen, seen + d.off_seen, static_cast<size_t>(4 * d.N + 1));
-    std::memcpy(po.J8.data() + d.off_J, couplings + d.off_J, static_cast<size_t>(2 * d.N));
-    std::memcpy(po.found.data() + d.off_found, lattices + d.off_found, static_cast<size_t>(d.n_int) * d.N);
-    for (int b = 0; b < d.n_int; ++b) {
-      po.fflag[d.off_fflag + b] = found[ob + b];
-      po.fflag[d.off_fflag + d.n_int + b] = found_energy[ob + b];
+  return wlg::guarded([&]() -> wlg_status {
+    if (ctx == nullptr || n < 0 ||
+        (n > 0 && (problems == nullptr || results == nullptr || seen == nullptr || couplings == nullptr ||
+                   found == nullptr || found_energy == nullptr || lattices == nullptr)))
+      return WLG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    ContextExec ex(ctx);
+    ex.h2d = ex.d2h = 0;
+    ex.launches = 0;
+    ex.main_forms = 0;
+    ex.t_pre = ex.t_main = 0;
+    ex.t_handoff = 0;
+    PreOut po;
+    int threads = 0, smem = 0;
+    std::string err;
+    wlg_status st = prerun_descs(problems, n, results, po, threads, smem, err);
+    if (st != WLG_OK) {
+      ctx->err = err;
+      return st;
     }
-    ob += d.n_int;
-  }
-  Prepared prep;
-  Handoff ho;
-  std::vector<MainResult> mres;
-  std::vector<double> out;
-  std::vector<int> win;
-  st = handoff(ex, problems, n, results, po, prep, ho);
-  if (st == WLG_OK) st = run_main(ex, results, prep, ho, mres, out, win, time_limit_s);
-  keep_stats(ctx, ex);
-  if (st != WLG_OK) return st;
-  return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+    long long ob = 0;
+    for (int p = 0; p < n; ++p) {
+      const PreDesc& d = po.pd[p];
+      std::memcpy(po.seen.data() + d.off_seen, seen + d.off_seen, static_cast<size_t>(4 * d.N + 1));
+      std::memcpy(po.J8.data() + d.off_J, couplings + d.off_J, static_cast<size_t>(2 * d.N));
+      std::memcpy(po.found.data() + d.off_found, lattices + d.off_found, static_cast<size_t>(d.n_int) * d.N);
+      for (int b = 0; b < d.n_int; ++b) {
+        po.fflag[d.off_fflag + b] = found[ob + b];
+        po.fflag[d.off_fflag + d.n_int + b] = found_energy[ob + b];
+      }
+      ob += d.n_int;
+    }
+    Prepared prep;
+    Handoff ho;
+    std::vector<MainResult> mres;
+    std::vector<double> out;
+    std::vector<int> win;
+    st = handoff(ex, problems, n, results, po, prep, ho);
+    if (st == WLG_OK) st = run_main(ex, results, prep, ho, mres, out, win, time_limit_s);
+    keep_stats(ctx, ex);
+    if (st != WLG_OK) return st;
+    return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+  });
 }
 
 wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, int n, int max_outer,
                                 wlg_tuning* out, int cap, int* n_out)
 {
-  if (ctx == nullptr || n <= 0 || problems == nullptr || max_outer <= 0 || (cap > 0 && out == nullptr))
-    return WLG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  std::vector<wlg_problem> probs(problems, problems + n);
-  for (wlg_problem& q : probs) q.max_outer = max_outer;
-  std::vector<wlg_result> res(static_cast<size_t>(n));
-  ContextExec ex(ctx);
-  Prepared prep;
-  Handoff ho;
-  wlg_status st = wlg::prepare_batch(ex, probs.data(), n, res.data(), prep, ho);
-  if (st != WLG_OK) {
-    ctx->err = ex.err;
-    return st;
-  }
-  // problems by (form, team size), as run_main groups them
-  std::map<std::pair<int, int>, std::vector<int>> groups;
-  for (size_t i = 0; i < prep.main.size(); ++i) {
-    const MainDesc& d = prep.main[i];
-    int form = main_form(d);
-    if (form == 0 && team_bytes(d, 0, d.team) > 227 * 1024) form = 3;
-    groups[{form == 3 ? 0 : form, d.team}].push_back(static_cast<int>(i));
-  }
-  std::map<std::pair<int, int>, int> best;
-  std::vector<wlg_tuning> found;
-  for (const auto& [key, idx] : groups) {
-    Prepared sub;
-    for (int i : idx) {
-      sub.main.push_back(prep.main[i]);
-      sub.main_problem.push_back(prep.main_problem[i]);
+  return wlg::guarded([&]() -> wlg_status {
+    if (ctx == nullptr || n <= 0 || problems == nullptr || max_outer <= 0 || (cap > 0 && out == nullptr))
+      return WLG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<wlg_problem> probs(problems, problems + n);
+    for (wlg_problem& q : probs) q.max_outer = max_outer;
+    std::vector<wlg_result> res(static_cast<size_t>(n));
+    ContextExec ex(ctx);
+    Prepared prep;
+    Handoff ho;
+    wlg_status st = wlg::prepare_batch(ex, probs.data(), n, res.data(), prep, ho);
+    if (st != WLG_OK) {
+      ctx->err = ex.err;
+      return st;
     }
-    const int limit = key.second <= 256 ? 256 / key.second : 1;
-    wlg_tuning t{key.first, key.second, 1, 0.0f, 0};
-    float best_ms = 0.0f;
-    for (int c = 1; c <= limit; c *= 2) {
-      std::map<std::pair<int, int>, int> force{{key, c}};
-      // the form recorded for the launch may be 3 when the team's state does
-      // not fit shared memory; force both keys
-      force[{3, key.second}] = c;
-      ex.per_cta = &force;
-      std::vector<MainResult> mres;
-      std::vector<double> out_host;
-      std::vector<int> win_host;
-      Prepared run = sub;
-      st = run_main(ex, res.data(), run, ho, mres, out_host, win_host, 0.0);
-      if (st != WLG_OK) {
-        ctx->err = ex.err;
-        return st;
-      }
-      if (c == 1 || ex.t_main < best_ms) {
-        best_ms = ex.t_main;
-        t.per_cta = c;
-      }
-      ++t.candidates;
+    // problems by (form, team size), as run_main groups them
+    std::map<std::pair<int, int>, std::vector<int>> groups;
+    for (size_t i = 0; i < prep.main.size(); ++i) {
+      const MainDesc& d = prep.main[i];
+      int form = main_form(d);
+      if (form == 0 && team_bytes(d, 0, d.team) > 227 * 1024) form = 3;
+      groups[{form == 3 ? 0 : form, d.team}].push_back(static_cast<int>(i));
     }
-    t.main_ms = best_ms;
-    best[key] = t.per_cta;
-    best[{3, key.second}] = t.per_cta;
-    found.push_back(t);
-  }
-  for (const auto& [k, v] : best) ctx->tuned[k] = v;
-  const int k = std::min(cap, static_cast<int>(found.size()));
-  for (int i = 0; i < k; ++i) out[i] = found[i];
-  if (n_out != nullptr) *n_out = static_cast<int>(found.size());
-  return WLG_OK;
+    std::map<std::pair<int, int>, int> best;
+    std::vector<wlg_tuning> found;
+    for (const auto& [key, idx] : groups) {
+      Prepared sub;
+      for (int i : idx) {
+        sub.main.push_back(prep.main[i]);
+        sub.main_problem.push_back(prep.main_problem[i]);
+      }
+      const int limit = key.second <= 256 ? 256 / key.second : 1;
+      wlg_tuning t{key.first, key.second, 1, 0.0f, 0};
+      float best_ms = 0.0f;
+      for (int c = 1; c <= limit; c *= 2) {
+        std::map<std::pair<int, int>, int> force{{key, c}};
+        // the form recorded for the launch may be 3 when the team's state does
+        // not fit shared memory; force both keys
+        force[{3, key.second}] = c;
+        ex.per_cta = &force;
+        std::vector<MainResult> mres;
+        std::vector<double> out_host;
+        std::vector<int> win_host;
+        Prepared run = sub;
+        st = run_main(ex, res.data(), run, ho, mres, out_host, win_host, 0.0);
+        if (st != WLG_OK) {
+          ctx->err = ex.err;
+          return st;
+        }
+        if (c == 1 || ex.t_main < best_ms) {
+          best_ms = ex.t_main;
+          t.per_cta = c;
+        }
+        ++t.candidates;
+      }
+      t.main_ms = best_ms;
+      best[key] = t.per_cta;
+      best[{3, key.second}] = t.per_cta;
+      found.push_back(t);
+    }
+    for (const auto& [k, v] : best) ctx->tuned[k] = v;
+    const int k = std::min(cap, static_cast<int>(found.size()));
+    for (int i = 0; i < k; ++i) out[i] = found[i];
+    if (n_out != nullptr) *n_out = static_cast<int>(found.size());
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)
@@ -1109,32 +1132,34 @@ wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)
 wlg_status wlg_class_log_probs(const int* energies, const double* log_g, const long long* offset, const int* count,
                                int n_classes, double prob, double* log_z, double* log_probs)
 {
-  if (n_classes <= 0 || prob <= 0 || prob >= 1 || energies == nullptr || log_g == nullptr) return WLG_ERR_INVALID;
-  const double beta_n = 0.5 * std::log((1.0 - prob) / prob);
-  std::vector<double> lz(static_cast<size_t>(n_classes));
-  for (int c = 0; c < n_classes; ++c) {
-    if (count[c] <= 0) return WLG_ERR_INVALID;
-    double mx = -std::numeric_limits<double>::infinity();
-    for (int i = 0; i < count[c]; ++i) {
-      const long long k = offset[c] + i;
-      mx = std::max(mx, log_g[k] - beta_n * energies[k]);
+  return wlg::guarded([&]() -> wlg_status {
+    if (n_classes <= 0 || prob <= 0 || prob >= 1 || energies == nullptr || log_g == nullptr) return WLG_ERR_INVALID;
+    const double beta_n = 0.5 * std::log((1.0 - prob) / prob);
+    std::vector<double> lz(static_cast<size_t>(n_classes));
+    for (int c = 0; c < n_classes; ++c) {
+      if (count[c] <= 0) return WLG_ERR_INVALID;
+      double mx = -std::numeric_limits<double>::infinity();
+      for (int i = 0; i < count[c]; ++i) {
+        const long long k = offset[c] + i;
+        mx = std::max(mx, log_g[k] - beta_n * energies[k]);
+      }
+      double s = 0;
+      for (int i = 0; i < count[c]; ++i) {
+        const long long k = offset[c] + i;
+        s += std::exp(log_g[k] - beta_n * energies[k] - mx);
+      }
+      lz[c] = mx + std::log(s);
     }
+    double mx = *std::max_element(lz.begin(), lz.end());
     double s = 0;
-    for (int i = 0; i < count[c]; ++i) {
-      const long long k = offset[c] + i;
-      s += std::exp(log_g[k] - beta_n * energies[k] - mx);
+    for (double v : lz) s += std::exp(v - mx);
+    const double lse = mx + std::log(s);
+    for (int c = 0; c < n_classes; ++c) {
+      if (log_z) log_z[c] = lz[c];
+      if (log_probs) log_probs[c] = lz[c] - lse;
     }
-    lz[c] = mx + std::log(s);
-  }
-  double mx = *std::max_element(lz.begin(), lz.end());
-  double s = 0;
-  for (double v : lz) s += std::exp(v - mx);
-  const double lse = mx + std::log(s);
-  for (int c = 0; c < n_classes; ++c) {
-    if (log_z) log_z[c] = lz[c];
-    if (log_probs) log_probs[c] = lz[c] - lse;
-  }
-  return WLG_OK;
+    return WLG_OK;
+  });
 }
 
 }  // extern "C"
@@ -1210,22 +1235,24 @@ wlg_status wlg_solve_raw_noalloc(const wlg_problem* problems, int n, wlg_result*
                                  int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset,
                                  wlg_stream stream)
 {
-  if (n < 0 || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
-  ArenaExec ex;
-  void* base = nullptr;
-  wlg_status st = wlg::noalloc_arena(&base, &ex.cap);
-  if (st != WLG_OK) return st;
-  ex.base = static_cast<unsigned char*>(base);
-  if (noalloc_bound(problems, n) > ex.cap) return WLG_ERR_CAPACITY;
-  cudaGetDevice(&ex.device);
-  ex.stream = wlg::as_stream(stream);
-  std::vector<MainResult> mres;
-  Prepared prep;
-  std::vector<double> out;
-  std::vector<int> win;
-  st = run_batch(ex, problems, n, results, mres, prep, out, win);
-  if (st != WLG_OK) return st;
-  return raw_windows(ex, problems, n, prep, out, win, win_start, win_end, raw_log_g, raw_capacity, raw_offset);
+  return wlg::guarded([&]() -> wlg_status {
+    if (n < 0 || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+    ArenaExec ex;
+    void* base = nullptr;
+    wlg_status st = wlg::noalloc_arena(&base, &ex.cap);
+    if (st != WLG_OK) return st;
+    ex.base = static_cast<unsigned char*>(base);
+    if (noalloc_bound(problems, n) > ex.cap) return WLG_ERR_CAPACITY;
+    cudaGetDevice(&ex.device);
+    ex.stream = wlg::as_stream(stream);
+    std::vector<MainResult> mres;
+    Prepared prep;
+    std::vector<double> out;
+    std::vector<int> win;
+    st = run_batch(ex, problems, n, results, mres, prep, out, win);
+    if (st != WLG_OK) return st;
+    return raw_windows(ex, problems, n, prep, out, win, win_start, win_end, raw_log_g, raw_capacity, raw_offset);
+  });
 }
 
 }  // extern "C"

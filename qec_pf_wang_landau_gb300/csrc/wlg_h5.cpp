@@ -631,6 +631,7 @@ std::string read_file(const std::string& path, Group& root)
 // ------------------------------------------------------------------ C ABI --
 
 #include "../../include/wlg.h"
+#include "wlg_internal.h"
 
 namespace {
 
@@ -672,51 +673,57 @@ unsigned int wlg_h5_lookup3(const void* data, size_t n, unsigned int init)
 
 wlg_status wlg_h5_list(const char* file, const char* group, char* names, size_t cap)
 {
-  if (file == nullptr || names == nullptr || cap == 0) return WLG_ERR_INVALID;
-  wlg::h5::Group root;
-  if (!wlg::h5::read_file(file, root).empty()) return WLG_ERR_INVALID;
-  const wlg::h5::Group* g;
-  const wlg::h5::Dataset* d;
-  if (!find(root, group, &g, &d).empty() || g == nullptr) return WLG_ERR_INVALID;
-  std::string out;
-  for (const auto& [k, v] : g->groups) out += k + "/\n";
-  for (const auto& [k, v] : g->datasets) out += k + "\n";
-  if (out.size() + 1 > cap) return WLG_ERR_CAPACITY;
-  std::memcpy(names, out.c_str(), out.size() + 1);
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (file == nullptr || names == nullptr || cap == 0) return WLG_ERR_INVALID;
+    wlg::h5::Group root;
+    if (!wlg::h5::read_file(file, root).empty()) return WLG_ERR_INVALID;
+    const wlg::h5::Group* g;
+    const wlg::h5::Dataset* d;
+    if (!find(root, group, &g, &d).empty() || g == nullptr) return WLG_ERR_INVALID;
+    std::string out;
+    for (const auto& [k, v] : g->groups) out += k + "/\n";
+    for (const auto& [k, v] : g->datasets) out += k + "\n";
+    if (out.size() + 1 > cap) return WLG_ERR_CAPACITY;
+    std::memcpy(names, out.c_str(), out.size() + 1);
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_h5_read(const char* file, const char* dataset, int* type, unsigned long long* count, void* buf,
                        unsigned long long cap_bytes)
 {
-  if (file == nullptr || dataset == nullptr || type == nullptr || count == nullptr) return WLG_ERR_INVALID;
-  wlg::h5::Group root;
-  if (!wlg::h5::read_file(file, root).empty()) return WLG_ERR_INVALID;
-  const wlg::h5::Group* g;
-  const wlg::h5::Dataset* d;
-  if (!find(root, dataset, &g, &d).empty() || d == nullptr) return WLG_ERR_INVALID;
-  *type = static_cast<int>(d->type);
-  *count = d->count;
-  if (buf != nullptr) {
-    if (d->bytes.size() > cap_bytes) return WLG_ERR_CAPACITY;
-    std::memcpy(buf, d->bytes.data(), d->bytes.size());
-  }
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (file == nullptr || dataset == nullptr || type == nullptr || count == nullptr) return WLG_ERR_INVALID;
+    wlg::h5::Group root;
+    if (!wlg::h5::read_file(file, root).empty()) return WLG_ERR_INVALID;
+    const wlg::h5::Group* g;
+    const wlg::h5::Dataset* d;
+    if (!find(root, dataset, &g, &d).empty() || d == nullptr) return WLG_ERR_INVALID;
+    *type = static_cast<int>(d->type);
+    *count = d->count;
+    if (buf != nullptr) {
+      if (d->bytes.size() > cap_bytes) return WLG_ERR_CAPACITY;
+      std::memcpy(buf, d->bytes.data(), d->bytes.size());
+    }
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_h5_attribute(const char* file, const char* dataset, const char* name, char* out, size_t cap)
 {
-  if (file == nullptr || dataset == nullptr || name == nullptr || out == nullptr || cap == 0) return WLG_ERR_INVALID;
-  wlg::h5::Group root;
-  if (!wlg::h5::read_file(file, root).empty()) return WLG_ERR_INVALID;
-  const wlg::h5::Group* g;
-  const wlg::h5::Dataset* d;
-  if (!find(root, dataset, &g, &d).empty() || d == nullptr) return WLG_ERR_INVALID;
-  auto it = d->string_attrs.find(name);
-  if (it == d->string_attrs.end()) return WLG_ERR_INVALID;
-  if (it->second.size() + 1 > cap) return WLG_ERR_CAPACITY;
-  std::memcpy(out, it->second.c_str(), it->second.size() + 1);
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (file == nullptr || dataset == nullptr || name == nullptr || out == nullptr || cap == 0) return WLG_ERR_INVALID;
+    wlg::h5::Group root;
+    if (!wlg::h5::read_file(file, root).empty()) return WLG_ERR_INVALID;
+    const wlg::h5::Group* g;
+    const wlg::h5::Dataset* d;
+    if (!find(root, dataset, &g, &d).empty() || d == nullptr) return WLG_ERR_INVALID;
+    auto it = d->string_attrs.find(name);
+    if (it == d->string_attrs.end()) return WLG_ERR_INVALID;
+    if (it->second.size() + 1 > cap) return WLG_ERR_CAPACITY;
+    std::memcpy(out, it->second.c_str(), it->second.size() + 1);
+    return WLG_OK;
+  });
 }
 
 }  // extern "C"

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <new>
+
 #include "../../include/wlg.h"
 
 namespace wlg {
@@ -21,6 +23,20 @@ inline wlg_status cuda_status(cudaError_t e)
   if (e == cudaSuccess) return WLG_OK;
   if (e == cudaErrorMemoryAllocation) return WLG_ERR_OOM;
   return WLG_ERR_CUDA;
+}
+
+// Runs an entry point's body so that no C++ exception crosses the C ABI:
+// allocation failures become WLG_ERR_OOM, anything else WLG_ERR_INVALID.
+template <typename F>
+wlg_status guarded(F&& body) noexcept
+{
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    return WLG_ERR_OOM;
+  } catch (...) {
+    return WLG_ERR_INVALID;
+  }
 }
 
 }  // namespace wlg

@@ -276,49 +276,51 @@ extern "C" {
 wlg_status wlg_solve_plain(const wlg_problem* problems, int n, wlg_result* results, int* energies, double* log_g,
                            long long capacity, wlg_stream stream, long long* kernel_launches)
 {
-  if (n < 0 || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
-  cudaStream_t s = wlg::as_stream(stream);
-  // group problems that differ only in the sample index; each group must hold
-  // samples 0..R-1 (one reference run)
-  std::map<std::vector<double>, std::vector<int>> groups;
-  for (int p = 0; p < n; ++p) {
-    const wlg_problem& q = problems[p];
-    std::vector<double> key = {static_cast<double>(q.X), static_cast<double>(q.Y), static_cast<double>(q.boundary),
-                               q.prob, static_cast<double>(q.error_class == 'I' ? 'i' : q.error_class),
-                               static_cast<double>(q.seed), static_cast<double>(q.pre_walkers),
-                               static_cast<double>(q.pre_intervals), static_cast<double>(q.pre_iterations),
-                               static_cast<double>(q.intervals), static_cast<double>(q.walkers_per_interval),
-                               q.overlap, q.alpha, q.beta, static_cast<double>(q.iterations),
-                               static_cast<double>(q.exchange_every), static_cast<double>(q.exchange_mode),
-                               static_cast<double>(q.global_parity), static_cast<double>(q.max_outer)};
-    groups[key].push_back(p);
-  }
-  long long pos = 0, launches = 0;
-  for (auto& [key, idx] : groups) {
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return problems[a].sample < problems[b].sample; });
-    for (size_t i = 0; i < idx.size(); ++i)
-      if (problems[idx[i]].sample != static_cast<int>(i)) return WLG_ERR_INVALID;
-    std::vector<wlg_result> res;
-    std::vector<std::vector<std::pair<int, double>>> curves;
-    WLG_TRY(run_plain(problems[idx[0]], static_cast<int>(idx.size()), s, res, curves, launches));
-    for (size_t i = 0; i < idx.size(); ++i) {
-      wlg_result r = res[i];
-      r.offset = pos;
-      r.n_energies = 0;
-      if (r.status == WLG_OK) {
-        if (pos + static_cast<long long>(curves[i].size()) > capacity) return WLG_ERR_CAPACITY;
-        for (size_t k = 0; k < curves[i].size(); ++k) {
-          energies[pos + static_cast<long long>(k)] = curves[i][k].first;
-          log_g[pos + static_cast<long long>(k)] = curves[i][k].second;
-        }
-        r.n_energies = static_cast<int>(curves[i].size());
-        pos += r.n_energies;
-      }
-      results[idx[i]] = r;
+  return wlg::guarded([&]() -> wlg_status {
+    if (n < 0 || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
+    cudaStream_t s = wlg::as_stream(stream);
+    // group problems that differ only in the sample index; each group must hold
+    // samples 0..R-1 (one reference run)
+    std::map<std::vector<double>, std::vector<int>> groups;
+    for (int p = 0; p < n; ++p) {
+      const wlg_problem& q = problems[p];
+      std::vector<double> key = {static_cast<double>(q.X), static_cast<double>(q.Y), static_cast<double>(q.boundary),
+                                 q.prob, static_cast<double>(q.error_class == 'I' ? 'i' : q.error_class),
+                                 static_cast<double>(q.seed), static_cast<double>(q.pre_walkers),
+                                 static_cast<double>(q.pre_intervals), static_cast<double>(q.pre_iterations),
+                                 static_cast<double>(q.intervals), static_cast<double>(q.walkers_per_interval),
+                                 q.overlap, q.alpha, q.beta, static_cast<double>(q.iterations),
+                                 static_cast<double>(q.exchange_every), static_cast<double>(q.exchange_mode),
+                                 static_cast<double>(q.global_parity), static_cast<double>(q.max_outer)};
+      groups[key].push_back(p);
     }
-  }
-  if (kernel_launches != nullptr) *kernel_launches = launches;
-  return WLG_OK;
+    long long pos = 0, launches = 0;
+    for (auto& [key, idx] : groups) {
+      std::sort(idx.begin(), idx.end(), [&](int a, int b) { return problems[a].sample < problems[b].sample; });
+      for (size_t i = 0; i < idx.size(); ++i)
+        if (problems[idx[i]].sample != static_cast<int>(i)) return WLG_ERR_INVALID;
+      std::vector<wlg_result> res;
+      std::vector<std::vector<std::pair<int, double>>> curves;
+      WLG_TRY(run_plain(problems[idx[0]], static_cast<int>(idx.size()), s, res, curves, launches));
+      for (size_t i = 0; i < idx.size(); ++i) {
+        wlg_result r = res[i];
+        r.offset = pos;
+        r.n_energies = 0;
+        if (r.status == WLG_OK) {
+          if (pos + static_cast<long long>(curves[i].size()) > capacity) return WLG_ERR_CAPACITY;
+          for (size_t k = 0; k < curves[i].size(); ++k) {
+            energies[pos + static_cast<long long>(k)] = curves[i][k].first;
+            log_g[pos + static_cast<long long>(k)] = curves[i][k].second;
+          }
+          r.n_energies = static_cast<int>(curves[i].size());
+          pos += r.n_energies;
+        }
+        results[idx[i]] = r;
+      }
+    }
+    if (kernel_launches != nullptr) *kernel_launches = launches;
+    return WLG_OK;
+  });
 }
 
 }  // extern "C"

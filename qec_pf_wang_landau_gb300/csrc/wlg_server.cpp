@@ -49,6 +49,7 @@
 #include <vector>
 
 #include "../../include/wlg.h"
+#include "wlg_internal.h"
 #include "wlg_batch.h"
 #include "wlg_engine.h"
 
@@ -727,10 +728,15 @@ void wlg_server::loop()
       continue;
     }
     bool busy = false;
-    busy |= retire();
-    busy |= do_reclaim();
-    busy |= admit();
-    busy |= launch();
+    try {
+      busy |= retire();
+      busy |= do_reclaim();
+      busy |= admit();
+      busy |= launch();
+    } catch (const std::exception& ex) {
+      fail_all(std::string("serving loop: ") + ex.what());
+      continue;
+    }
     long long resident = 0;
     for (const auto& [k, g] : groups) resident += static_cast<long long>(g.members.size());
     {
@@ -745,66 +751,72 @@ extern "C" {
 
 wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_server** out)
 {
-  if (out == nullptr) return WLG_ERR_INVALID;
-  *out = nullptr;
-  int count = 0;
-  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return WLG_ERR_CUDA;
-  auto s = std::make_unique<wlg_server>();
-  s->device = device;
-  if (config != nullptr) s->cfg = *config;
-  if (s->cfg.mem_budget_bytes == 0) s->cfg.mem_budget_bytes = size_t{1} << 30;
-  if (s->cfg.epoch_outer <= 0) s->cfg.epoch_outer = 4;
-  if (s->cfg.max_prerun_batch <= 0) s->cfg.max_prerun_batch = 256;
-  if (s->cfg.max_resident <= 0) s->cfg.max_resident = 8192;
-  if (s->cfg.max_resident < kClasses) return WLG_ERR_INVALID;
-  s->t0 = Clock::now();
-  const wlg_status st = s->setup();
-  if (st != WLG_OK) {
-    s->teardown();
-    return st;
-  }
-  wlg_server* raw = s.release();
-  raw->th = std::thread([raw] { raw->loop(); });
-  *out = raw;
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (out == nullptr) return WLG_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return WLG_ERR_CUDA;
+    auto s = std::make_unique<wlg_server>();
+    s->device = device;
+    if (config != nullptr) s->cfg = *config;
+    if (s->cfg.mem_budget_bytes == 0) s->cfg.mem_budget_bytes = size_t{1} << 30;
+    if (s->cfg.epoch_outer <= 0) s->cfg.epoch_outer = 4;
+    if (s->cfg.max_prerun_batch <= 0) s->cfg.max_prerun_batch = 256;
+    if (s->cfg.max_resident <= 0) s->cfg.max_resident = 8192;
+    if (s->cfg.max_resident < kClasses) return WLG_ERR_INVALID;
+    s->t0 = Clock::now();
+    const wlg_status st = s->setup();
+    if (st != WLG_OK) {
+      s->teardown();
+      return st;
+    }
+    wlg_server* raw = s.release();
+    raw->th = std::thread([raw] { raw->loop(); });
+    *out = raw;
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_server_submit(wlg_server* server, const wlg_problem* requests, int n, unsigned long long* ids)
 {
-  if (server == nullptr || n < 0 || (n > 0 && (requests == nullptr || ids == nullptr))) return WLG_ERR_INVALID;
-  for (int i = 0; i < n; ++i) {
-    wlg_problem q = requests[i];
-    q.error_class = 'i';
-    if (check_problem(q) != WLG_OK || q.prob <= 0.0f || q.prob >= 1.0f) return WLG_ERR_INVALID;
-  }
-  std::lock_guard<std::mutex> lk(server->mu);
-  const double t = server->now_ms();
-  for (int i = 0; i < n; ++i) {
-    Request r;
-    r.q = requests[i];
-    r.out.submit_ms = t;
-    ids[i] = server->next_id++;
-    r.out.id = ids[i];
-    server->incoming.emplace_back(ids[i], std::move(r));
-    ++server->stats.submitted;
-  }
-  server->cv_in.notify_all();
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (server == nullptr || n < 0 || (n > 0 && (requests == nullptr || ids == nullptr))) return WLG_ERR_INVALID;
+    for (int i = 0; i < n; ++i) {
+      wlg_problem q = requests[i];
+      q.error_class = 'i';
+      if (check_problem(q) != WLG_OK || q.prob <= 0.0f || q.prob >= 1.0f) return WLG_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(server->mu);
+    const double t = server->now_ms();
+    for (int i = 0; i < n; ++i) {
+      Request r;
+      r.q = requests[i];
+      r.out.submit_ms = t;
+      ids[i] = server->next_id++;
+      r.out.id = ids[i];
+      server->incoming.emplace_back(ids[i], std::move(r));
+      ++server->stats.submitted;
+    }
+    server->cv_in.notify_all();
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_server_poll(wlg_server* server, wlg_decoded* out, int cap, int* n_out, int timeout_ms)
 {
-  if (server == nullptr || n_out == nullptr || cap < 0 || (cap > 0 && out == nullptr)) return WLG_ERR_INVALID;
-  std::unique_lock<std::mutex> lk(server->mu);
-  if (server->finished.empty() && timeout_ms > 0)
-    server->cv_out.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !server->finished.empty(); });
-  int k = 0;
-  while (k < cap && !server->finished.empty()) {
-    out[k++] = server->finished.front();
-    server->finished.pop_front();
-  }
-  *n_out = k;
-  return WLG_OK;
+  return wlg::guarded([&]() -> wlg_status {
+    if (server == nullptr || n_out == nullptr || cap < 0 || (cap > 0 && out == nullptr)) return WLG_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(server->mu);
+    if (server->finished.empty() && timeout_ms > 0)
+      server->cv_out.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !server->finished.empty(); });
+    int k = 0;
+    while (k < cap && !server->finished.empty()) {
+      out[k++] = server->finished.front();
+      server->finished.pop_front();
+    }
+    *n_out = k;
+    return WLG_OK;
+  });
 }
 
 wlg_status wlg_server_stats_get(const wlg_server* server, wlg_server_stats* out)

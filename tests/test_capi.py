@@ -86,6 +86,8 @@ def test_invalid_arguments_rejected_without_gpu(engine):
     assert L.wlg_server_submit(None, None, 0, None) == 1
     assert L.wlg_server_poll(None, None, 0, None, 0) == 1
     assert L.wlg_server_destroy(None) == 1
+    assert L.wlg_context_set_stream(None, None) == 1
+    assert L.wlg_solve(None, None, 0, None, None, None, 0) == 1
 
 
 def test_server_without_a_device_fails_cleanly(engine):

@@ -253,6 +253,24 @@ def test_autotune_picks_teams_per_cta_without_changing_results(cuda):
         assert np.array_equal(E1, E2) and np.array_equal(G1, G2)
 
 
+def test_solve_on_a_caller_stream(cuda):
+    """wlg_context_set_stream: solves run on the caller's stream with the same results."""
+    import qec_pf_wang_landau_gb300 as wlg
+    torch = cuda
+    probs = [wlg.problem(5, 5, prob=0.05, error_class=c, seed=3, sample=k, intervals=6, beta=0.02, iterations=500)
+             for k in range(4) for c in "iv"]
+    ctx = wlg.Context(0)
+    a = ctx.solve(probs)
+    s = torch.cuda.Stream()
+    ctx.set_stream(s.cuda_stream)
+    b = ctx.solve(probs)
+    ctx.set_stream(None)
+    c = ctx.solve(probs)
+    for (r1, E1, G1), (r2, E2, G2), (r3, E3, G3) in zip(a, b, c):
+        assert r1.status == r2.status == r3.status
+        assert np.array_equal(G1, G2) and np.array_equal(G1, G3) and np.array_equal(E1, E2)
+
+
 def test_engine_4x4_log_g_against_exact_enumeration(cuda):
     """Config 1 (4x4 periodic, p=0.04, seed 12345, class i): the normalised log g
     against exact FP64 enumeration of all 2^16 states."""
