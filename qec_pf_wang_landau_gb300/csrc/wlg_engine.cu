@@ -323,6 +323,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   uint32_t* Js = reinterpret_cast<uint32_t*>(base + lay.off_J);
   ulonglong2* nbt = reinterpret_cast<ulonglong2*>(base + lay.off_nbt);
   double* fwin = reinterpret_cast<double*>(base + lay.off_f);
+  double* lnfw = fwin + d.I;  // log(f) of each window, recomputed only when f changes
   int* cond = reinterpret_cast<int*>(base + lay.off_cond);
   int* flat = reinterpret_cast<int*>(base + lay.off_flat);
   int* win = reinterpret_cast<int*>(base + lay.off_win);  // start, end, base, Lb, E0
@@ -339,6 +340,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   for (int q = t; q < 5 * I; q += P) win[q] = winpool[d.off_win + q];
   for (int q = t; q < I; q += P) {
     fwin[q] = kE;
+    lnfw[q] = log(kE);
     cond[q] = 0;
     flat[q] = 0;
   }
@@ -420,6 +422,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     counter = hdr[1];
     if (t < I) {
       fwin[t] = reinterpret_cast<const double*>(st + sl.off_f)[t];
+      lnfw[t] = log(fwin[t]);
       cond[t] = reinterpret_cast<const int*>(st + sl.off_cond)[t];
     }
     perm[t] = reinterpret_cast<const int*>(st + sl.off_perm)[t];
@@ -462,7 +465,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     const unsigned wmask = __ballot_sync(0xFFFFFFFFu, live);
     if (live) {
       const bool frozen = cond[b] != 0;
-      const double lnf = log(fwin[b]);
+      const double lnf = lnfw[b];  // log(f) (wl.cu:1124)
       const float lnf_f = static_cast<float>(lnf);
       int c_cur = (E - bb) >> d.lg;
       double g_cur = G[c_cur * P + t];
@@ -472,7 +475,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       // rate) small
       const double gbase = g_cur;
       const Split gbase_split = split_float(gbase);
-      for (int c = 0; c < d.L; ++c) Gf[c * P + t] = static_cast<float>(G[c * P + t] - gbase);
+      for (int c = 0; c < d.L; ++c) Gf[c * P + t] = shadow_split(G[c * P + t], gbase_split);
       // one rounding of a double of size |g| <= |gbase| + (small shadow terms)
       const float ulp_g = static_cast<float>((fabs(gbase) + 1.0) * 0x1p-51);
       float gfb = 0.0f;               // float of g_cur - gbase at the last change of bin
@@ -641,6 +644,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     team.sync();
     if (t < I && cond[t] == 0 && flat[t] == W) {
       fwin[t] = sqrt(fwin[t]);
+      lnfw[t] = log(fwin[t]);
       cond[t] = 1;
     }
     team.sync();

@@ -143,8 +143,8 @@ WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, b
   o = align16(o + 4 * 2 * nwL);
   t.off_nbt = o;
   o = align16(o + 16 * nbt_sites);
-  t.off_f = o;
-  o = align16(o + 8 * I);
+  t.off_f = o;  // f [I], then ln f [I]
+  o = align16(o + 16 * I);
   t.off_cond = o;
   o = align16(o + 4 * I);
   t.off_flat = o;
