@@ -162,6 +162,144 @@ def accuracy(out, ref_runs):
     return summary
 
 
+SERVING = dict(rate=200.0, seconds=1.0, side_min=4, side_max=16, prob_min=0.02, prob_max=0.12, beta=1e-6,
+               walkers_per_interval=4, wait_s=120.0, seed=2026)
+
+
+def serving_requests(n_max: int = 100000):
+    """Poisson arrival times and decoding requests of the serving workload:
+    square periodic lattices with side uniform in {4..16}, p uniform in
+    [0.02, 0.12], ln f 1e-6, windows scaled with N (N/16, 4..16), 4 walkers
+    each, pre-run 128 walkers x 100 N iterations; all four classes per
+    request (the server runs them)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = SERVING
+    rng = np.random.default_rng(c["seed"])
+    t, arrivals, reqs = 0.0, [], []
+    while len(reqs) < n_max:
+        t += rng.exponential(1.0 / c["rate"])
+        if t > c["seconds"]:
+            break
+        L = int(rng.integers(c["side_min"], c["side_max"] + 1))
+        N = L * L
+        arrivals.append(t)
+        reqs.append(wlg.problem(L, L, prob=float(rng.uniform(c["prob_min"], c["prob_max"])), seed=c["seed"],
+                                sample=len(reqs), pre_walkers=128, pre_intervals=32, pre_iterations=100 * N,
+                                intervals=int(min(16, max(4, N // 16))), walkers_per_interval=c["walkers_per_interval"],
+                                overlap=0.25, alpha=0.8, beta=c["beta"], iterations=1000, exchange_every=10))
+    return arrivals, reqs
+
+
+def serving_run():
+    """The serving workload through wlg_server: requests submitted at their
+    Poisson arrival times, latency = retirement - submission (server clock)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    arrivals, reqs = serving_requests()
+    got, ids = {}, []
+    with wlg.Server(0) as srv:
+        t0 = time.perf_counter()
+        for a, q in zip(arrivals, reqs):
+            delay = t0 + a - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids += srv.submit([q])
+            for d in srv.poll(256, 0):
+                got[int(d.id)] = d
+        while len(got) < len(ids) and time.perf_counter() - t0 < SERVING["wait_s"]:
+            for d in srv.poll(256, 50):
+                got[int(d.id)] = d
+        st = srv.stats()
+    done = [got[i] for i in ids if i in got]
+    lat = np.array([d.done_ms - d.submit_ms for d in done]) if done else np.zeros(1)
+    span_s = (max(d.done_ms for d in done) - min(d.submit_ms for d in done)) / 1e3 if done else float("nan")
+    statuses = {}
+    for d in done:
+        statuses[str(d.status)] = statuses.get(str(d.status), 0) + 1
+    return {"workload": "Poisson 200 req/s for 1 s, side U{4..16} periodic, p U[0.02,0.12], ln f 1e-6, "
+                        "4 classes per request, W=4, I=N/16 in [4,16]",
+            "requests": len(ids), "retired": len(done), "retired_ok": statuses.get("0", 0), "status_counts": statuses,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "throughput_req_s": len(done) / span_s if done else 0.0,
+            "epochs": st["epochs"], "prerun_launches": st["prerun_launches"],
+            "note": f"requests not retired within {SERVING['wait_s']:.0f} s are left out of the percentiles"}
+
+
+BATCHED = dict(samples=2000, sides=(4, 6, 8, 10, 12), prob_min=0.02, prob_max=0.12, beta=1e-6, seed=31337)
+
+
+def batched_problems():
+    """The heterogeneous batched workload: 2000 disorder samples, side
+    uniform in {4,6,8,10,12}, boundary periodic/open 50/50, p uniform in
+    [0.02, 0.12], class uniform over i/v/h/c, windows 8..32 scaled with N,
+    4 walkers each, overlap 0.25, flatness 0.8, ln f 1e-6; per-sample
+    parameters from a seeded host generator, disorder from Philox."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = BATCHED
+    rng = np.random.default_rng(c["seed"])
+    out = []
+    for k in range(c["samples"]):
+        L = int(rng.choice(c["sides"]))
+        N = L * L
+        out.append(wlg.problem(L, L, boundary=int(rng.integers(0, 2)), prob=float(rng.uniform(c["prob_min"], c["prob_max"])),
+                               error_class="ivhc"[int(rng.integers(0, 4))], seed=c["seed"], sample=k, pre_walkers=128,
+                               pre_intervals=32, pre_iterations=100 * N, intervals=int(min(32, max(8, N // 8))),
+                               walkers_per_interval=4, overlap=0.25, alpha=0.8, beta=c["beta"], iterations=1000,
+                               exchange_every=10))
+    return out
+
+
+def batched_run():
+    """The heterogeneous batch in one wlg_solve call: converged samples/s."""
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = batched_problems()
+    ctx = wlg.Context(0)
+    t0 = time.perf_counter()
+    out = ctx.solve(probs)
+    wall = time.perf_counter() - t0
+    st = ctx.stats()
+    dev_s = (st["pre_ms"] + st["handoff_ms"] + st["main_ms"]) / 1e3
+    counts = {}
+    for r, _, _ in out:
+        counts[str(r.status)] = counts.get(str(r.status), 0) + 1
+    flips = sum(r.flips for r, _, _ in out)
+    return {"workload": "2000 samples, side U{4,6,8,10,12}, open/periodic 50/50, p U[0.02,0.12], class U{ivhc}, "
+                        "I = N/8 in [8,32], W=4, o=0.25, alpha=0.8, ln f 1e-6, exchange every 10",
+            "value": counts.get("0", 0) / dev_s, "unit": "samples/s", "e2e_samples_per_s": counts.get("0", 0) / wall,
+            "status_counts": counts, "flips_per_s": flips / (st["main_ms"] / 1e3), "pre_ms": st["pre_ms"],
+            "main_ms": st["main_ms"], "main_forms": st["main_forms"], "kernel_launches": st["kernel_launches"]}
+
+
+LARGE = dict(sides=(16, 24), samples=38, prob=0.10, seed=4242, max_outer=10)
+
+
+def large_run():
+    """The large-lattice workload (16x16 and 24x24 periodic, p = 0.10, all four
+    classes, 64 windows x 8 walkers, overlap 0.3, exchange every 10, ln f 1e-8),
+    bounded: one wave of 38 samples x 4 classes per side, each capped at 10
+    outer iterations (a run to ln f 1e-8 takes hours).  Reports the WL flip
+    rate and the step time of the 512-thread teams."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = LARGE
+    out = {"workload": "16x16 and 24x24 periodic, p=0.10, classes ivhc, I=64 x W=8, o=0.3, alpha=0.8, ln f 1e-8, "
+                       "exchange every 10; 38 samples x 4 classes per side, capped at 10 outer iterations"}
+    ctx = wlg.Context(0)
+    for L in c["sides"]:
+        N = L * L
+        probs = [wlg.problem(L, L, prob=c["prob"], error_class=cl, seed=c["seed"], sample=k, pre_walkers=128,
+                             pre_intervals=128, pre_iterations=100 * N, intervals=64, walkers_per_interval=8,
+                             overlap=0.3, alpha=0.8, beta=1e-8, iterations=1000, exchange_every=10,
+                             max_outer=c["max_outer"]) for k in range(c["samples"]) for cl in "ivhc"]
+        res = ctx.solve_raw(probs)
+        st = ctx.stats()
+        flips = sum(r.flips for r, _, _, _ in res)
+        outer = max(r.outer_iterations for r, _, _, _ in res)
+        out[f"{L}x{L}"] = {"problems": len(probs), "flips_per_s": flips / (st["main_ms"] / 1e3),
+                           "main_ms": st["main_ms"], "pre_ms": st["pre_ms"],
+                           "us_per_step": st["main_ms"] * 1e3 / (outer * 1000), "main_forms": st["main_forms"],
+                           "ran": sum(1 for r, _, _, _ in res if r.status in (0, 7))}
+    return out
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:

@@ -7,9 +7,11 @@
 // host thread:
 //
 //   admit   - pending requests whose worst-case device memory fits the
-//             budget get arena blocks and table slots; one pre-run launch
-//             and the host hand-off (prepare_batch, the batch engine's own
-//             code) prepare them, and their main-run inputs are uploaded;
+//             budget get arena blocks; an admission thread runs their
+//             pre-run (one launch on its own stream) and the host hand-off
+//             (prepare_batch, the batch engine's own code) while the loop
+//             keeps launching epochs; then the loop gives them table slots
+//             and uploads their main-run inputs;
 //   launch  - every resident problem advances in "epochs": main-run launches
 //             of at most `epoch_outer` outer iterations that suspend each
 //             unfinished problem's state (walkers, histograms, log g, RNG
@@ -223,6 +225,21 @@ struct Group {
   cudaEvent_t ev[kRing] = {};
 };
 
+// One admission: requests with reserved arena blocks, prepared (pre-run +
+// hand-off) by the admission thread while the loop keeps launching epochs.
+struct AdmitJob {
+  std::vector<std::pair<unsigned long long, Request>> batch;
+  std::vector<size_t> block_off;
+  std::vector<BlockLayout> bound;
+  std::vector<wlg_problem> qs;
+  std::vector<wlg_result> res;
+  Prepared prep;
+  Handoff ho;
+  wlg_status st = WLG_OK;
+  std::string err;
+  bool done = false;  // under wlg_server::amu
+};
+
 }  // namespace
 
 struct wlg_server {
@@ -256,12 +273,22 @@ struct wlg_server {
   std::deque<std::pair<unsigned long long, Request>> pending;
   std::vector<cudaEvent_t> admit_ev;
   std::vector<int> reclaim;  // finished slots waiting for their epochs
-  std::unique_ptr<GrowExec> pre;
+  std::unique_ptr<GrowExec> pre;  // used by the admission thread only
   int sms = 1;
+
+  // admission thread: pre-run + hand-off of one job at a time
+  std::thread admitter;
+  std::mutex amu;
+  std::condition_variable acv;
+  AdmitJob* a_todo = nullptr;
+  bool a_stop = false;
+  std::unique_ptr<AdmitJob> job;  // the loop's job in flight, if any
 
   double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
   void loop();
   bool admit();
+  void finish_admission(AdmitJob& j);
+  void admit_worker();
   bool launch();
   bool retire();
   bool do_reclaim();
@@ -408,13 +435,28 @@ void wlg_server::class_done(unsigned long long id, int cls, int status, long lon
   }
 }
 
-// Pending requests -> pre-run + hand-off -> arena blocks -> groups.
+// Pending requests -> reserved arena blocks -> the admission thread; a
+// prepared job -> uploads -> groups.
 bool wlg_server::admit()
 {
-  if (pending.empty()) return false;
-  std::vector<std::pair<unsigned long long, Request>> batch;
-  std::vector<size_t> block_off;
-  std::vector<BlockLayout> bound;
+  bool any = false;
+  if (job) {
+    bool ready;
+    {
+      std::lock_guard<std::mutex> lk(amu);
+      ready = job->done;
+    }
+    if (!ready) return false;
+    std::unique_ptr<AdmitJob> j = std::move(job);
+    finish_admission(*j);
+    any = true;
+    if (fatal) return true;
+  }
+  if (pending.empty()) return any;
+  auto nj = std::make_unique<AdmitJob>();
+  std::vector<std::pair<unsigned long long, Request>>& batch = nj->batch;
+  std::vector<size_t>& block_off = nj->block_off;
+  std::vector<BlockLayout>& bound = nj->bound;
   while (!pending.empty() && static_cast<int>(batch.size()) < cfg.max_prerun_batch &&
          static_cast<int>(free_slots.size()) >= kClasses * static_cast<int>(batch.size() + 1)) {
     const BlockLayout bl = block_bound(pending.front().second.q);
@@ -424,7 +466,7 @@ bool wlg_server::admit()
       if (!arena.alloc(bl.bytes, &offs[got])) break;
     if (got < kClasses) {
       for (int c = 0; c < got; ++c) arena.release(offs[c], bl.bytes);
-      if (active.empty() && batch.empty()) {  // can never fit
+      if (active.empty() && batch.empty() && reclaim.empty()) {  // can never fit
         auto [id, r] = std::move(pending.front());
         pending.pop_front();
         r.out.id = id;
@@ -445,25 +487,64 @@ bool wlg_server::admit()
     batch.push_back(std::move(pending.front()));
     pending.pop_front();
   }
-  if (batch.empty()) return false;
+  if (batch.empty()) return any;
   const int n = static_cast<int>(batch.size()) * kClasses;
-  std::vector<wlg_problem> qs(static_cast<size_t>(n));
+  nj->qs.resize(static_cast<size_t>(n));
   for (size_t i = 0; i < batch.size(); ++i)
     for (int c = 0; c < kClasses; ++c) {
-      qs[i * kClasses + c] = batch[i].second.q;
-      qs[i * kClasses + c].error_class = kClassName[c];
+      nj->qs[i * kClasses + c] = batch[i].second.q;
+      nj->qs[i * kClasses + c].error_class = kClassName[c];
     }
-  std::vector<wlg_result> res(static_cast<size_t>(n));
-  Prepared prep;
-  Handoff ho;
-  const wlg_status st = prepare_batch(*pre, qs.data(), n, res.data(), prep, ho);
+  nj->res.resize(static_cast<size_t>(n));
+  job = std::move(nj);
+  {
+    std::lock_guard<std::mutex> lk(amu);
+    a_todo = job.get();
+  }
+  acv.notify_all();
+  return true;
+}
+
+void wlg_server::admit_worker()
+{
+  cudaSetDevice(device);
+  for (;;) {
+    AdmitJob* j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(amu);
+      acv.wait(lk, [&] { return a_stop || a_todo != nullptr; });
+      if (a_todo == nullptr) return;  // stopping with nothing to do
+      j = a_todo;
+      a_todo = nullptr;
+    }
+    j->st = prepare_batch(*pre, j->qs.data(), static_cast<int>(j->qs.size()), j->res.data(), j->prep, j->ho);
+    j->err = pre->err;
+    std::lock_guard<std::mutex> lk(amu);
+    j->done = true;
+  }
+}
+
+// A prepared job: blocks, uploads, group membership, immediate results.
+void wlg_server::finish_admission(AdmitJob& aj)
+{
+  std::vector<std::pair<unsigned long long, Request>>& batch = aj.batch;
+  const std::vector<size_t>& block_off = aj.block_off;
+  const std::vector<BlockLayout>& bound = aj.bound;
+  const int n = static_cast<int>(aj.qs.size());
+  std::vector<wlg_result>& res = aj.res;
+  Prepared& prep = aj.prep;
+  Handoff& ho = aj.ho;
+  const wlg_status st = aj.st;
+  if (batch.empty()) return;
   {
     std::lock_guard<std::mutex> lk(mu);
     ++stats.prerun_launches;
   }
   if (st != WLG_OK) {
-    fail_all("pre-run: " + pre->err);
-    return true;
+    for (size_t k = 0; k < block_off.size(); ++k) arena.release(block_off[k], bound[k].bytes);
+    for (auto& [id, r] : batch) active.emplace(id, std::move(r));
+    fail_all("pre-run: " + aj.err);
+    return;
   }
   for (auto& [id, r] : batch) active.emplace(id, std::move(r));
   // which batch problems reach the main run
@@ -472,7 +553,7 @@ bool wlg_server::admit()
   cudaEvent_t ev = nullptr;
   if (!cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming))) {
     fail_all("event");
-    return true;
+    return;
   }
   const int ev_index = static_cast<int>(admit_ev.size());
   admit_ev.push_back(ev);
@@ -528,7 +609,7 @@ bool wlg_server::admit()
     ok = ok && cuda_ok(cudaMemsetAsync(d_res + slot, 0, sizeof(MainResult), s_pre));
     if (!ok) {
       fail_all("upload");
-      return true;
+      return;
     }
     auto key = std::make_pair(form, d.team);
     Group& g = groups[key];
@@ -545,7 +626,7 @@ bool wlg_server::admit()
       }
       if (!ok) {
         fail_all("group setup");
-        return true;
+        return;
       }
     }
     pr.group = key;
@@ -555,11 +636,10 @@ bool wlg_server::admit()
   // memory have left `host` when they return)
   if (!cuda_ok(cudaEventRecord(ev, s_pre))) {
     fail_all("event record");
-    return true;
+    return;
   }
   std::lock_guard<std::mutex> lk(mu);
   stats.bytes_in_use = static_cast<long long>(arena.used());
-  return true;
 }
 
 // One epoch per group with resident problems and fewer than two in flight.
@@ -714,7 +794,7 @@ void wlg_server::loop()
   while (!stop.load()) {
     {
       std::unique_lock<std::mutex> lk(mu);
-      const bool idle = incoming.empty() && pending.empty() && active.empty() && reclaim.empty();
+      const bool idle = incoming.empty() && pending.empty() && active.empty() && reclaim.empty() && !job;
       if (idle) cv_in.wait_for(lk, std::chrono::milliseconds(2), [&] { return stop.load() || !incoming.empty(); });
       while (!incoming.empty()) {
         pending.push_back(std::move(incoming.front()));
@@ -771,6 +851,7 @@ wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_se
       return st;
     }
     wlg_server* raw = s.release();
+    raw->admitter = std::thread([raw] { raw->admit_worker(); });
     raw->th = std::thread([raw] { raw->loop(); });
     *out = raw;
     return WLG_OK;
@@ -840,6 +921,12 @@ wlg_status wlg_server_destroy(wlg_server* server)
   server->stop.store(true);
   server->cv_in.notify_all();
   if (server->th.joinable()) server->th.join();
+  {
+    std::lock_guard<std::mutex> lk(server->amu);
+    server->a_stop = true;
+  }
+  server->acv.notify_all();
+  if (server->admitter.joinable()) server->admitter.join();
   server->teardown();
   delete server;
   return WLG_OK;

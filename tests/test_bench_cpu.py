@@ -1,0 +1,45 @@
+"""bench.py on CPU: every leg the JSON line reports exists, and the synthetic
+workloads follow their specifications (no GPU needed to build them)."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_legs_exist():
+    import bench
+    for name in ("run_ours", "run_reference", "serving_run", "batched_run", "large_run", "accuracy", "plain_run",
+                 "reference_cuda_run", "cpu_run", "profile_case", "reduce_over_ranks"):
+        assert callable(getattr(bench, name)), name
+
+
+def test_headline_workload():
+    import bench
+    probs = bench.problems(0)
+    assert len(probs) == 400
+    assert {(p.X, p.Y, p.boundary, round(p.prob, 6)) for p in probs} == {(6, 6, 0, 0.04)}
+    assert sorted({p.sample for p in probs}) == list(range(100))
+    assert {(p.intervals, p.walkers_per_interval, p.iterations, p.exchange_every) for p in probs} == {(10, 3, 1000, 20)}
+
+
+def test_serving_workload_is_poisson_at_200_per_second():
+    import bench
+    arrivals, reqs = bench.serving_requests()
+    assert 120 < len(reqs) < 280  # 200 expected in 1 s
+    gaps = np.diff([0.0] + arrivals)
+    assert abs(gaps.mean() - 1 / 200) < 0.0015
+    assert {r.X for r in reqs} <= set(range(4, 17)) and all(r.X == r.Y for r in reqs)
+    assert all(0.02 <= r.prob <= 0.12 and r.beta == 1e-6 and r.boundary == 0 for r in reqs)
+
+
+def test_batched_workload():
+    import bench
+    probs = bench.batched_problems()
+    assert len(probs) == 2000
+    assert {p.X for p in probs} == {4, 6, 8, 10, 12}
+    assert {p.boundary for p in probs} == {0, 1}
+    assert {p.error_class for p in probs} == {b"i", b"v", b"h", b"c"}
+    assert all(8 <= p.intervals <= 32 and p.walkers_per_interval == 4 and p.beta == 1e-6 for p in probs)
