@@ -291,6 +291,32 @@ def test_engine_4x4_log_g_against_exact_enumeration(cuda):
     assert np.abs(err).max() < 0.6
 
 
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_engine_8x8_log_g_and_class_probabilities_against_exact(cuda, boundary):
+    """8x8 (2^64 states) by the oracle's transfer matrix: the engine's stitched
+    log g has exactly the reachable energies and WL-size errors, and the four
+    class probabilities at the Nishimori temperature match the exact ones."""
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = [wlg.problem(8, 8, boundary=boundary, prob=0.08, error_class=c, seed=31, sample=0, pre_walkers=128,
+                         pre_intervals=32, pre_iterations=6400, intervals=8, walkers_per_interval=4, beta=1e-4,
+                         iterations=1000, exchange_every=5) for c in "ivhc"]
+    out = wlg.Context(0).solve(probs)
+    assert all(r.status == 0 for r, _, _ in out)
+    exact_lz = []
+    bn = 0.5 * np.log(0.92 / 0.08)
+    for (r, E, G), c in zip(out, "ivhc"):
+        J = O.init_interactions(8, 8, 1, 31, 0.08, c)
+        cnt = O.exact_counts(J, 8, 8, boundary)
+        assert set(E.tolist()) == set((np.nonzero(cnt)[0] - 128).tolist())
+        err = G - np.log(cnt[E + 128])
+        assert np.sqrt(np.mean(err ** 2)) < 0.5 and np.abs(err).max() < 1.5
+        Ee = np.nonzero(cnt)[0] - 128
+        exact_lz.append(np.logaddexp.reduce(np.log(cnt[Ee + 128]) - bn * Ee))
+    exact_lp = np.array(exact_lz) - np.logaddexp.reduce(exact_lz)
+    _, lp = wlg.class_log_probs([(E, G) for _, E, G in out], 0.08)
+    assert np.abs(np.exp(lp) - np.exp(exact_lp)).max() < 0.05
+
+
 def test_class_log_probs_normalised(cuda):
     import qec_pf_wang_landau_gb300 as wlg
     probs = [wlg.problem(4, 4, prob=0.1, error_class=c, seed=77, sample=0, pre_walkers=32, pre_intervals=8,
