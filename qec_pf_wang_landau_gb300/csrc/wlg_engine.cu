@@ -506,9 +506,12 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       int ovr_acc = -1;   // exact acceptance of the step being replayed
       int q = static_cast<int>(pos - (blk << 2));  // draw offset in block A, 0..3
       uint64_t nc = blk + 2;                        // counter of the block being built in C
-      for (;;) {
+      // For the first n_iter warp iterations no live lane has finished (a
+      // lane finishes after n_iter committed steps), so the warp votes on
+      // continuing only after that, when lanes that replayed catch up.
+      for (int k = 0;; ++k) {
         const bool act = it < d.n_iter && !stopped;
-        if (!__any_sync(wmask, act)) break;
+        if (k >= d.n_iter && !__any_sync(wmask, act)) break;
         {
           const uint4 half = philox_rounds<5>(Cb, phase == 0 ? rng.k0 : k5a, phase == 0 ? rng.k1 : k5b);
           Cb = phase < 2 ? half : Cb;
