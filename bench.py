@@ -460,7 +460,7 @@ def run_ours(args):
                      "basis": f"{BYTES_PER_FLIP} algorithmic B per WL flip of the main-run kernel, per launch / "
                               "the launch's event-timed duration",
                      "note": "walker state is on-chip (traffic 0.8 MB per launch against ~34 GB algorithmic); "
-                             "the step is one warp's dependent chain, 38% issue-active per warp"},
+                             "the step is one warp's dependent chain, 40% issue-active per warp"},
         "cpu_baseline": {"value": cpu_pps, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
                          "flips_per_s": cpu_fps,
                          "sample": f"{CPU_SAMPLE_PROBLEMS} problems of the same workload (samples 0-23 x ivhc), "
