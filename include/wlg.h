@@ -199,9 +199,12 @@ typedef struct {
 typedef struct wlg_context wlg_context;
 
 /* A context owns a CUDA stream and the device buffers of the engine on
- * `device`.  mem_budget_bytes = 0 means no limit beyond the device's. */
+ * `device`.  mem_budget_bytes = 0 means no limit beyond the device's.  A
+ * context serves one host thread at a time (calls on it must not overlap);
+ * use one context per thread for concurrent solves. */
 wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context** out);
 wlg_status wlg_context_destroy(wlg_context* ctx);
+/* Text of the last failure on ctx; valid until the next call on ctx. */
 const char* wlg_context_last_error(const wlg_context* ctx);
 /* Later solves on ctx run on `stream` (NULL: the context's own stream);
  * work already queued on the previous stream is finished first.  Solves
@@ -369,6 +372,7 @@ wlg_status wlg_server_poll(wlg_server* server, wlg_decoded* out, int cap, int* n
 wlg_status wlg_server_stats_get(const wlg_server* server, wlg_server_stats* out);
 /* Stops the loop (unfinished requests are dropped) and frees everything. */
 wlg_status wlg_server_destroy(wlg_server* server);
+/* Text of the failure that stopped the server ("" while it runs). */
 const char* wlg_server_last_error(const wlg_server* server);
 
 /* ---- HDF5 result files without libhdf5 (the prerun/mainrun programs write
