@@ -345,6 +345,7 @@ typedef struct {
   int epoch_outer;         /* outer WL iterations per main-run launch; 0: 4 */
   int max_prerun_batch;    /* requests per pre-run launch; 0: 256 */
   int max_resident;        /* resident problems (4 per request); 0: 8192 */
+  int fail_after_epochs;   /* testing: a host-side failure is injected after this many epochs; 0: never */
 } wlg_server_config;
 
 typedef struct {

@@ -268,7 +268,8 @@ def class_log_probs(curves, prob):
 # ----------------------------------------------------------------- serving --
 
 class ServerConfig(C.Structure):
-    _fields_ = [("mem_budget_bytes", sz), ("epoch_outer", i32), ("max_prerun_batch", i32), ("max_resident", i32)]
+    _fields_ = [("mem_budget_bytes", sz), ("epoch_outer", i32), ("max_prerun_batch", i32), ("max_resident", i32),
+                ("fail_after_epochs", i32)]
 
 
 class Decoded(C.Structure):
@@ -287,8 +288,8 @@ class Server:
     poll retired requests with their four class log-probabilities."""
 
     def __init__(self, device: int = 0, mem_budget_bytes: int = 0, epoch_outer: int = 0, max_prerun_batch: int = 0,
-                 max_resident: int = 0):
-        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident)
+                 max_resident: int = 0, fail_after_epochs: int = 0):
+        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident, fail_after_epochs)
         h = C.c_void_p()
         call("wlg_server_create", device, C.byref(cfg), C.byref(h))
         self._h = h

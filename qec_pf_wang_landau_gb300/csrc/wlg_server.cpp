@@ -365,22 +365,21 @@ void wlg_server::fail_all(const std::string& why)
     std::lock_guard<std::mutex> lk(mu);
     err = why;
   }
-  for (auto& [id, r] : active) {
+  auto retire_failed = [&](Request& r) {
     r.out.status = WLG_ERR_CUDA;
     r.out.done_ms = now_ms();
     std::lock_guard<std::mutex> lk(mu);
     finished.push_back(r.out);
     ++stats.completed;
-  }
+  };
+  for (auto& [id, r] : active) retire_failed(r);
   active.clear();
-  for (auto& [id, r] : pending) {
-    r.out.status = WLG_ERR_CUDA;
-    r.out.done_ms = now_ms();
-    std::lock_guard<std::mutex> lk(mu);
-    finished.push_back(r.out);
-    ++stats.completed;
-  }
+  for (auto& [id, r] : pending) retire_failed(r);
   pending.clear();
+  if (job) {  // an admission in flight: its thread reads only the job's copies of the parameters
+    for (auto& [id, r] : job->batch) retire_failed(r);
+    job->batch.clear();
+  }
   cv_out.notify_all();
 }
 
@@ -646,6 +645,10 @@ void wlg_server::finish_admission(AdmitJob& aj)
 bool wlg_server::launch()
 {
   bool any = false;
+  if (cfg.fail_after_epochs > 0 && stats.epochs >= cfg.fail_after_epochs) {  // injected (testing)
+    fail_all("injected failure after " + std::to_string(cfg.fail_after_epochs) + " epochs");
+    return true;
+  }
   for (auto& [key, g] : groups) {
     if (g.members.empty() || static_cast<int>(g.inflight.size()) >= kMaxInFlight) continue;
     const int n = static_cast<int>(g.members.size());

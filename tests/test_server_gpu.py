@@ -154,3 +154,22 @@ def test_global_pool_form_resumes_exactly(cuda):
     assert max(outer) > 3
     if d.status == 0:
         assert np.array_equal(np.array(d.log_probs), lp)
+
+
+def test_failure_retires_every_request_and_server_stays_usable(cuda):
+    """A failure in the serving loop (injected on the host after 3 epochs; no
+    GPU fault) retires every admitted and pending request with WLG_ERR_CUDA,
+    later submissions fail the same way, and poll/stats/destroy keep working."""
+    import qec_pf_wang_landau_gb300 as wlg
+    # beta 1e-6 needs about 20 halvings of ln f, each at least one outer iteration
+    reqs = [request(wlg, X, Y, k, boundary=b, beta=1e-6, intervals=4)
+            for k, (X, Y, b) in enumerate([(4, 4, 0), (5, 5, 1), (6, 6, 0), (4, 4, 1), (5, 5, 0), (6, 6, 1)])]
+    with wlg.Server(0, epoch_outer=1, fail_after_epochs=3) as srv:
+        ids = srv.submit(reqs)
+        got = srv.wait(ids, 120)
+        assert all(got[i].status == 2 for i in ids)
+        assert "injected failure" in wlg.lib().wlg_server_last_error(srv._h).decode()
+        (late,) = srv.submit([reqs[0]])
+        assert srv.wait([late], 60)[late].status == 2
+        st = srv.stats()
+        assert st["completed"] == len(ids) + 1 and st["epochs"] >= 3
