@@ -221,6 +221,37 @@ wlg_status wlg_context_set_stream(wlg_context* ctx, wlg_stream stream);
 wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* energies,
                      double* log_g, long long capacity);
 
+/* wlg_solve on given disorder (no counterpart in the reference, which
+ * always draws it, wl.cu:364-386): couplings holds each problem's class-'i'
+ * bond pattern, +-1, 2*X*Y entries per problem, problems concatenated, in
+ * the reference's layout (right bonds [i*Y + j] then down bonds
+ * [N + i*Y + j], wl.cu:77-87; the wrap-around bonds are unused with open
+ * boundaries).  The problem's error_class still applies its logical chain
+ * on top (prerun.cu:56-75); prob is not used for the bonds.  Every random
+ * stream except the disorder is the one wlg_solve uses, so couplings equal
+ * to the drawn ones give wlg_solve's results bit for bit.  NULL couplings:
+ * wlg_solve. */
+wlg_status wlg_solve_couplings(wlg_context* ctx, const wlg_problem* problems, int n, const signed char* couplings,
+                               wlg_result* results, int* energies, double* log_g, long long capacity);
+
+/* Syndromes of bond patterns (the decoding front-end; no counterpart in
+ * the reference).  Plaquette (i, j) has corners (i, j), (i, j+1), (i+1, j),
+ * (i+1, j+1) and is frustrated when
+ * J_right(i, j) J_right(i+1, j) J_down(i, j) J_down(i, j+1) = -1; periodic
+ * lattices have X*Y plaquettes (indices mod X, Y), open ones (X-1)*(Y-1),
+ * row-major.  wlg_frustration writes syndrome[plaquette] = 1 for frustrated
+ * plaquettes, else 0.  wlg_couplings_from_syndrome writes a +-1 pattern with
+ * exactly the given frustrated plaquettes: every defect is moved along its
+ * row to column 0 and then (periodic) along column 0 to plaquette (0, 0),
+ * where defects cancel in pairs, or (open) out across the left edge; the
+ * bonds crossed are -1.  A periodic syndrome with an odd number of defects
+ * has no pattern (WLG_ERR_INVALID).  Decoding a syndrome: its pattern's
+ * four error classes (wlg_server_submit_couplings) give the log-probability
+ * of each logical class relative to the pattern. */
+wlg_status wlg_frustration(int X, int Y, int boundary, const signed char* couplings, unsigned char* syndrome);
+wlg_status wlg_couplings_from_syndrome(int X, int Y, int boundary, const unsigned char* syndrome,
+                                       signed char* couplings);
+
 /* Like wlg_solve, without stitching: the walker-0 log g of every window on
  * the reference's dense per-window layout (window b covers energies
  * win_start..win_end, zeros at unreachable energies), problem after
@@ -367,6 +398,11 @@ wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_se
 /* Queues n requests; ids[i] receives request i's id.  Invalid requests are
  * rejected whole (WLG_ERR_INVALID, nothing queued). */
 wlg_status wlg_server_submit(wlg_server* server, const wlg_problem* requests, int n, unsigned long long* ids);
+/* wlg_server_submit on given disorder: couplings as wlg_solve_couplings
+ * (the class-'i' pattern of each request, 2*X*Y entries, concatenated);
+ * the four classes apply their chains on top.  NULL: wlg_server_submit. */
+wlg_status wlg_server_submit_couplings(wlg_server* server, const wlg_problem* requests, int n,
+                                       const signed char* couplings, unsigned long long* ids);
 /* Up to `cap` finished requests in completion order; waits up to timeout_ms
  * (0: no wait) for at least one.  *n_out = 0 when none finished in time. */
 wlg_status wlg_server_poll(wlg_server* server, wlg_decoded* out, int cap, int* n_out, int timeout_ms);

@@ -46,6 +46,9 @@ SIGNATURES = {
     "wlg_context_last_error": [P],
     "wlg_context_set_stream": [P, P],
     "wlg_solve": [P, P, i32, P, P, P, i64],
+    "wlg_solve_couplings": [P, P, i32, P, P, P, P, i64],
+    "wlg_frustration": [i32, i32, i32, P, P],
+    "wlg_couplings_from_syndrome": [i32, i32, i32, P, P],
     "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
     "wlg_last_stats": [P, P],
     "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
@@ -60,6 +63,7 @@ SIGNATURES = {
     "wlg_context_autotune": [P, P, i32, i32, P, i32, P],
     "wlg_server_create": [i32, P, P],
     "wlg_server_submit": [P, P, i32, P],
+    "wlg_server_submit_couplings": [P, P, i32, P, P],
     "wlg_server_poll": [P, P, i32, P, i32],
     "wlg_server_stats_get": [P, P],
     "wlg_server_destroy": [P],
@@ -68,6 +72,44 @@ SIGNATURES = {
 _RESTYPE = {"wlg_status_string": C.c_char_p, "wlg_version": C.c_char_p, "wlg_context_last_error": C.c_char_p,
             "wlg_h5_lookup3": u32,
             "wlg_server_last_error": C.c_char_p}
+
+
+def _couplings(problems, couplings):
+    """Concatenated int8 bond patterns (None stays None)."""
+    if couplings is None:
+        return None
+    import numpy as np
+    parts = [np.ascontiguousarray(c, dtype=np.int8).ravel() for c in couplings]
+    if len(parts) != len(problems) or any(len(c) != 2 * p.X * p.Y for c, p in zip(parts, problems)):
+        raise ValueError("one bond pattern of 2*X*Y entries per problem")
+    return np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros(1, np.int8))
+
+
+def plaquettes(X: int, Y: int, boundary: int) -> int:
+    """Number of plaquettes of an X x Y lattice (X*Y periodic, (X-1)*(Y-1) open)."""
+    return X * Y if boundary == 0 else (X - 1) * (Y - 1)
+
+
+def frustration(X: int, Y: int, boundary: int, couplings):
+    """Syndrome (uint8 per plaquette, row-major) of a +-1 bond pattern (wlg_frustration)."""
+    import numpy as np
+    J = np.ascontiguousarray(couplings, dtype=np.int8).ravel()
+    if len(J) != 2 * X * Y:
+        raise ValueError("bond pattern needs 2*X*Y entries")
+    out = np.zeros(max(plaquettes(X, Y, boundary), 1), np.uint8)
+    call("wlg_frustration", X, Y, boundary, J.ctypes.data_as(P), out.ctypes.data_as(P))
+    return out[:plaquettes(X, Y, boundary)]
+
+
+def couplings_from_syndrome(X: int, Y: int, boundary: int, syndrome):
+    """A +-1 bond pattern whose frustrated plaquettes are the syndrome (wlg_couplings_from_syndrome)."""
+    import numpy as np
+    S = np.ascontiguousarray(syndrome, dtype=np.uint8).ravel()
+    if len(S) != plaquettes(X, Y, boundary):
+        raise ValueError("syndrome needs one entry per plaquette")
+    J = np.zeros(2 * X * Y, np.int8)
+    call("wlg_couplings_from_syndrome", X, Y, boundary, S.ctypes.data_as(P), J.ctypes.data_as(P))
+    return J
 
 
 class WlgError(RuntimeError):
@@ -154,8 +196,10 @@ class Context:
             detail = lib().wlg_context_last_error(self._h).decode()
             raise WlgError(name, st, f"{lib().wlg_status_string(st).decode()}: {detail}")
 
-    def solve(self, problems):
-        """Stitched, normalised log g per problem: list of (Result, energies, log_g) (numpy arrays)."""
+    def solve(self, problems, couplings=None):
+        """Stitched, normalised log g per problem: list of (Result, energies, log_g) (numpy arrays).
+        couplings: None (drawn from seed and sample) or one class-'i' bond pattern (+-1, 2*X*Y) per
+        problem (wlg_solve_couplings)."""
         import numpy as np
         n = len(problems)
         arr = (Problem * n)(*problems)
@@ -163,8 +207,10 @@ class Context:
         cap = sum(4 * p.X * p.Y + 1 for p in problems)
         E = np.zeros(max(cap, 1), np.int32)
         G = np.zeros(max(cap, 1), np.float64)
-        self._check("wlg_solve", lib().wlg_solve(self._h, C.cast(arr, P), n, C.cast(res, P), E.ctypes.data_as(P),
-                                                  G.ctypes.data_as(P), cap))
+        J = _couplings(problems, couplings)
+        self._check("wlg_solve_couplings",
+                    lib().wlg_solve_couplings(self._h, C.cast(arr, P), n, None if J is None else J.ctypes.data_as(P),
+                                              C.cast(res, P), E.ctypes.data_as(P), G.ctypes.data_as(P), cap))
         out = []
         for r in res:
             a, b = r.offset, r.offset + r.n_energies
@@ -294,12 +340,16 @@ class Server:
         call("wlg_server_create", device, C.byref(cfg), C.byref(h))
         self._h = h
 
-    def submit(self, requests):
-        """Queue requests (Problems; error_class ignored); returns their ids."""
+    def submit(self, requests, couplings=None):
+        """Queue requests (Problems; error_class ignored); returns their ids.  couplings: None (drawn)
+        or one class-'i' bond pattern (+-1, 2*X*Y) per request (wlg_server_submit_couplings)."""
         n = len(requests)
         arr = (Problem * n)(*requests)
         ids = (u64 * max(n, 1))()
-        self._check("wlg_server_submit", lib().wlg_server_submit(self._h, C.cast(arr, P), n, C.cast(ids, P)))
+        J = _couplings(requests, couplings)
+        self._check("wlg_server_submit_couplings",
+                    lib().wlg_server_submit_couplings(self._h, C.cast(arr, P), n,
+                                                      None if J is None else J.ctypes.data_as(P), C.cast(ids, P)))
         return [int(ids[i]) for i in range(n)]
 
     def poll(self, cap: int = 256, timeout_ms: int = 0):

@@ -139,13 +139,18 @@ struct PreOut {
 wlg_status prerun_descs(const wlg_problem* probs, int n, wlg_result* results, PreOut& po, int& threads, int& smem,
                         std::string& err);
 // Validation and the pre-run of every problem (one launch).
-wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, PreOut& po);
+// couplings (int8 [sum 2N], problem order): the class-'i' bond patterns of the
+// problems whose given[p] != 0 (all of them when given is null); the others
+// draw theirs.  Null couplings: every problem draws.
+wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, PreOut& po,
+                      const int8_t* couplings = nullptr, const unsigned char* given = nullptr);
 // The hand-off to the main run on the host.  Problems that cannot start the
 // main run get their status in `results` and no MainDesc.
 wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, const PreOut& po, Prepared& prep,
                    Handoff& ho);
 // run_prerun + handoff.
-wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho);
+wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho,
+                         const int8_t* couplings = nullptr, const unsigned char* given = nullptr);
 
 // Main-run form of a problem by lattice storage: 0 spins in shared memory,
 // 1 spins in a register, 2 register spins + neighbour table (X, Y >= 3);

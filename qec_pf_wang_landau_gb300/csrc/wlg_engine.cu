@@ -64,8 +64,13 @@ __global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ 
   int8_t* lat = J + 2 * N;  // [walkers][N]
 
   const int tid = threadIdx.x;
-  // disorder (wl.cu:364-386) and error chain (wl.cu:388-428, prerun.cu:56-75)
+  // disorder (wl.cu:364-386), or the caller's pattern, and the error chain
+  // (wl.cu:388-428, prerun.cu:56-75)
   for (int q = tid; q < 2 * N; q += blockDim.x) {
+    if (d.given_J) {
+      J[q] = Jpool[d.off_J + q];
+      continue;
+    }
     Stream st;
     st.init(key_size(d.seed, static_cast<uint64_t>(d.sample)), 0, static_cast<uint64_t>(q));
     const double u = st.uniform();

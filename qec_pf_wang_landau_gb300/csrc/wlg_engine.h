@@ -28,6 +28,7 @@ struct PreDesc {
   int n_int;        // coarse bins for stored lattices
   int len_int;      // coarse bin width (interval.cpp with overlap 1)
   int n_iter;
+  int given_J;          // 1: the class-'i' couplings are read from off_J instead of drawn
   long long off_J;      // int8 [2N]
   long long off_seen;   // uint8 [4N+1]
   long long off_found;  // int8 [n_int][N]

@@ -362,7 +362,8 @@ wlg_status prerun_descs(const wlg_problem* probs, int n, wlg_result* results, Pr
   return WLG_OK;
 }
 
-wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, PreOut& po)
+wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, PreOut& po,
+                      const int8_t* couplings, const unsigned char* given)
 {
   ex.h2d = ex.d2h = 0;
   ex.launches = 0;
@@ -373,7 +374,20 @@ wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* res
   std::string err;
   wlg_status st = prerun_descs(probs, n, results, po, threads, smem, err);
   if (st != WLG_OK) return fail(ex, st, err);
-  const std::vector<PreDesc>& pd = po.pd;
+  std::vector<PreDesc>& pd = po.pd;
+  bool any_given = false;
+  if (couplings != nullptr)
+    for (int p = 0; p < n; ++p) {
+      if (given != nullptr && given[p] == 0) continue;
+      PreDesc& d = pd[p];
+      for (int q = 0; q < 2 * d.N; ++q) {
+        const int8_t v = couplings[d.off_J + q];
+        if (v != 1 && v != -1) return fail(ex, WLG_ERR_INVALID, "couplings of problem " + std::to_string(p) + " not +-1");
+        po.J8[d.off_J + q] = v;
+      }
+      d.given_J = 1;
+      any_given = true;
+    }
   const long long oJ = static_cast<long long>(po.J8.size()), oS = static_cast<long long>(po.seen.size());
   const long long oF = static_cast<long long>(po.found.size()), oG = static_cast<long long>(po.fflag.size());
   void *d_pd = nullptr, *d_J8 = nullptr, *d_seen = nullptr, *d_found = nullptr, *d_fflag = nullptr;
@@ -383,6 +397,11 @@ wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* res
   if ((st = ex.buffer(kFound, static_cast<size_t>(oF), &d_found)) != WLG_OK) return st;
   if ((st = ex.buffer(kFflag, static_cast<size_t>(oG) * sizeof(int), &d_fflag)) != WLG_OK) return st;
   cudaMemsetAsync(d_found, 0, static_cast<size_t>(oF), ex.stream);
+  if (any_given) {
+    if (cudaMemcpyAsync(d_J8, po.J8.data(), static_cast<size_t>(oJ), cudaMemcpyHostToDevice, ex.stream) != cudaSuccess)
+      return fail(ex, WLG_ERR_CUDA, "couplings upload failed");
+    ex.h2d += oJ;
+  }
   if (ex.ev != nullptr) cudaEventRecord(ex.ev[0], ex.stream);
   st = wlg::launch_pre_batch(static_cast<const PreDesc*>(d_pd), n, threads, smem, static_cast<int8_t*>(d_J8),
                              static_cast<uint8_t*>(d_seen), static_cast<int8_t*>(d_found), static_cast<int*>(d_fflag),
@@ -566,10 +585,11 @@ wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* result
   return WLG_OK;
 }
 
-wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho)
+wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho,
+                         const int8_t* couplings, const unsigned char* given)
 {
   PreOut po;
-  const wlg_status st = run_prerun(ex, probs, n, results, po);
+  const wlg_status st = run_prerun(ex, probs, n, results, po, couplings, given);
   if (st != WLG_OK) return st;
   return handoff(ex, probs, n, results, po, prep, ho);
 }
@@ -750,10 +770,10 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
 // The whole batch up to the main-run results.
 wlg_status run_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results,
                      std::vector<MainResult>& mres, Prepared& prep, std::vector<double>& out_host,
-                     std::vector<int>& win_host)
+                     std::vector<int>& win_host, const int8_t* couplings = nullptr)
 {
   Handoff ho;
-  const wlg_status st = wlg::prepare_batch(ex, probs, n, results, prep, ho);
+  const wlg_status st = wlg::prepare_batch(ex, probs, n, results, prep, ho, couplings);
   if (st != WLG_OK) return st;
   return run_main(ex, results, prep, ho, mres, out_host, win_host, 0.0);
 }
@@ -949,6 +969,12 @@ extern "C" {
 wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* energies,
                      double* log_g, long long capacity)
 {
+  return wlg_solve_couplings(ctx, problems, n, nullptr, results, energies, log_g, capacity);
+}
+
+wlg_status wlg_solve_couplings(wlg_context* ctx, const wlg_problem* problems, int n, const signed char* couplings,
+                               wlg_result* results, int* energies, double* log_g, long long capacity)
+{
   return wlg::guarded([&]() -> wlg_status {
     if (ctx == nullptr || (n > 0 && (problems == nullptr || results == nullptr))) return WLG_ERR_INVALID;
     cudaSetDevice(ctx->device);
@@ -957,7 +983,7 @@ wlg_status wlg_solve(wlg_context* ctx, const wlg_problem* problems, int n, wlg_r
     std::vector<double> out;
     std::vector<int> win;
     ContextExec ex(ctx);
-    wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win);
+    wlg_status st = run_batch(ex, problems, n, results, mres, prep, out, win, reinterpret_cast<const int8_t*>(couplings));
     keep_stats(ctx, ex);
     if (st != WLG_OK) return st;
     return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);

@@ -198,6 +198,7 @@ struct Problem {
 
 struct Request {
   wlg_problem q{};
+  std::vector<int8_t> J;  // given class-'i' couplings (2N), empty: drawn
   wlg_decoded out{};
   int remaining = kClasses;
   int status[kClasses] = {};
@@ -232,6 +233,8 @@ struct AdmitJob {
   std::vector<size_t> block_off;
   std::vector<BlockLayout> bound;
   std::vector<wlg_problem> qs;
+  std::vector<int8_t> J;             // given couplings in problem order (empty: all drawn)
+  std::vector<unsigned char> given;  // per problem
   std::vector<wlg_result> res;
   Prepared prep;
   Handoff ho;
@@ -494,6 +497,19 @@ bool wlg_server::admit()
       nj->qs[i * kClasses + c] = batch[i].second.q;
       nj->qs[i * kClasses + c].error_class = kClassName[c];
     }
+  bool any_given = false;
+  for (const auto& [id, r] : batch) any_given |= !r.J.empty();
+  if (any_given)
+    for (size_t i = 0; i < batch.size(); ++i)
+      for (int c = 0; c < kClasses; ++c) {
+        const Request& r = batch[i].second;
+        const size_t twoN = 2 * static_cast<size_t>(r.q.X) * r.q.Y;
+        if (r.J.empty())
+          nj->J.insert(nj->J.end(), twoN, 1);
+        else
+          nj->J.insert(nj->J.end(), r.J.begin(), r.J.end());
+        nj->given.push_back(r.J.empty() ? 0 : 1);
+      }
   nj->res.resize(static_cast<size_t>(n));
   job = std::move(nj);
   {
@@ -516,7 +532,8 @@ void wlg_server::admit_worker()
       j = a_todo;
       a_todo = nullptr;
     }
-    j->st = prepare_batch(*pre, j->qs.data(), static_cast<int>(j->qs.size()), j->res.data(), j->prep, j->ho);
+    j->st = prepare_batch(*pre, j->qs.data(), static_cast<int>(j->qs.size()), j->res.data(), j->prep, j->ho,
+                          j->J.empty() ? nullptr : j->J.data(), j->given.empty() ? nullptr : j->given.data());
     j->err = pre->err;
     std::lock_guard<std::mutex> lk(amu);
     j->done = true;
@@ -863,18 +880,30 @@ wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_se
 
 wlg_status wlg_server_submit(wlg_server* server, const wlg_problem* requests, int n, unsigned long long* ids)
 {
+  return wlg_server_submit_couplings(server, requests, n, nullptr, ids);
+}
+
+wlg_status wlg_server_submit_couplings(wlg_server* server, const wlg_problem* requests, int n,
+                                       const signed char* couplings, unsigned long long* ids)
+{
   return wlg::guarded([&]() -> wlg_status {
     if (server == nullptr || n < 0 || (n > 0 && (requests == nullptr || ids == nullptr))) return WLG_ERR_INVALID;
+    std::vector<size_t> off_J(static_cast<size_t>(n) + 1, 0);
     for (int i = 0; i < n; ++i) {
       wlg_problem q = requests[i];
       q.error_class = 'i';
       if (check_problem(q) != WLG_OK || q.prob <= 0.0f || q.prob >= 1.0f) return WLG_ERR_INVALID;
+      off_J[i + 1] = off_J[i] + 2 * static_cast<size_t>(q.X) * q.Y;
     }
+    if (couplings != nullptr)
+      for (size_t k = 0; k < off_J[n]; ++k)
+        if (couplings[k] != 1 && couplings[k] != -1) return WLG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(server->mu);
     const double t = server->now_ms();
     for (int i = 0; i < n; ++i) {
       Request r;
       r.q = requests[i];
+      if (couplings != nullptr) r.J.assign(couplings + off_J[i], couplings + off_J[i + 1]);
       r.out.submit_ms = t;
       ids[i] = server->next_id++;
       r.out.id = ids[i];
