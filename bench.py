@@ -148,7 +148,7 @@ def accuracy(out, ref_runs):
                 n = C.c_int(0)
                 rc = O.lib().orc_stitch(O.ptr(np.ascontiguousarray(flat)), O.ptr(np.ascontiguousarray(run["start"][k * I:])),
                                         O.ptr(np.ascontiguousarray(run["end"][k * I:])), I, 1, X, Y, O.ptr(Er),
-                                        O.ptr(Gr), len(Er), C.byref(n))
+                                        O.ptr(Gr), len(Er), C.byref(n), 0)
                 if rc == 0:
                     e = Gr[:n.value] - np.log(cnt[Er[:n.value] + 2 * N])
                     res["reference_cuda"].append((float(np.sqrt(np.mean(e ** 2))), float(np.abs(e).max())))

@@ -211,6 +211,19 @@ const char* wlg_context_last_error(const wlg_context* ctx);
  * still return after their stream has reached the results. */
 wlg_status wlg_context_set_stream(wlg_context* ctx, wlg_stream stream);
 
+/* How stitching picks the energy where window i hands over to a later window
+ * (result_handling.cpp:115-143): the shared energy whose slopes towards the
+ * next energy agree best.  At a window's last energy there is no next one;
+ * the reference reads past the end of its std::map there (:125-126), which
+ * with libstdc++ yields a phantom successor whose energy is the window's
+ * number of entries and whose value is ~0.  WLG_STITCH_REFERENCE (the
+ * default) uses that phantom and so writes the reference's output bins;
+ * WLG_STITCH_DEFINED skips energies without a successor. */
+enum { WLG_STITCH_REFERENCE = 0, WLG_STITCH_DEFINED = 1 };
+/* Stitching mode of later solves on ctx (wlg_solve, wlg_solve_couplings,
+ * wlg_mainrun). */
+wlg_status wlg_context_set_stitching(wlg_context* ctx, int mode);
+
 /* Runs pre-run and main run of n problems as one batch on the GPU and
  * returns each problem's stitched, normalised log g (result_handling.cpp,
  * logsumexp = X*Y*ln 2): pairs (energies[i], log_g[i]) for i in
@@ -377,6 +390,7 @@ typedef struct {
   int max_prerun_batch;    /* requests per pre-run launch; 0: 256 */
   int max_resident;        /* resident problems (4 per request); 0: 8192 */
   int fail_after_epochs;   /* testing: a host-side failure is injected after this many epochs; 0: never */
+  int stitching;           /* WLG_STITCH_REFERENCE (0) or WLG_STITCH_DEFINED */
 } wlg_server_config;
 
 typedef struct {

@@ -76,7 +76,7 @@ def _declare(L):
         "orc_prerun": (None, [i32, i32, i32, f32, C.c_char, i32, i32, i32, i32, i32, P, P, P, P, P]),
         "orc_mainrun": (i32, [i32, i32, i32, i32, i32, i32, f32, f64, f64, i32, i32, i32, i32, i32, i64] + [P] * 5
                         + [i32] + [P] * 8),
-        "orc_stitch": (i32, [P, P, P, i32, i32, i32, i32, P, P, i32, P]),
+        "orc_stitch": (i32, [P, P, P, i32, i32, i32, i32, P, P, i32, P, i32]),
         "orc_exact_counts": (None, [P, i32, i32, i32, P]),
         "orc_enumerate_counts": (None, [P, i32, i32, i32, P]),
         "orc_log_partition": (f64, [P, P, i32, f64]),
@@ -193,6 +193,65 @@ def reference_harness():
             raise RuntimeError(f"reference cubin could not be loaded (code {rc})")
         _ref = L
     return _ref
+
+
+_ref_host = None
+
+
+def reference_host():
+    """ctypes handle of oracle/_ref/libref_host.so (the reference's own
+    interval.cpp and result_handling.cpp), or None where the reference
+    sources are absent."""
+    global _ref_host
+    if _ref_host is None:
+        from . import ref_build
+        so = ref_build.build_host()
+        if so is None:
+            return None
+        L = C.CDLL(so)
+        L.ref_interval.argtypes = [i32, i32, C.c_uint, i32, f32, P, P, P, P]
+        L.ref_interval.restype = C.c_int
+        L.ref_stitch.argtypes = [P, i64, P, P, i32, i32, i32, i32, P, P, i32, P]
+        L.ref_stitch.restype = C.c_int
+        _ref_host = L
+    return _ref_host
+
+
+def ref_interval(e_min, e_max, n_int, walkers, overlap):
+    """interval.cpp of the reference: (starts, ends, total, len) or None when it throws."""
+    L = reference_host()
+    s = np.zeros(n_int, np.int32)
+    e = np.zeros(n_int, np.int32)
+    tot, ln = C.c_longlong(0), C.c_int(0)
+    if L.ref_interval(e_min, e_max, n_int, walkers, C.c_float(overlap), ptr(s), ptr(e), C.byref(tot), C.byref(ln)):
+        return None
+    return s, e, tot.value, ln.value
+
+
+def ref_stitch(logG, start, end, n_int, W, X, Y):
+    """result_handling.cpp of the reference: (rc, E, log g) it would write."""
+    L = reference_host()
+    cap = 4 * X * Y + 1 + 4 * n_int
+    E = np.zeros(cap, np.int32)
+    G = np.zeros(cap, np.float64)
+    n = C.c_int(0)
+    lg = np.ascontiguousarray(logG, np.float64)
+    s, e = np.ascontiguousarray(start, np.int32), np.ascontiguousarray(end, np.int32)
+    rc = L.ref_stitch(ptr(lg), len(lg), ptr(s), ptr(e), n_int, W, X, Y, ptr(E), ptr(G), cap, C.byref(n))
+    return rc, E[:n.value].copy(), G[:n.value].copy()
+
+
+def stitch(logG, start, end, n_int, W, X, Y, mode=0):
+    """The oracle's restatement of result_handling.cpp: (rc, E, log g).
+    mode 0: the reference's phantom successor at a window's last key; 1: skipped."""
+    cap = 4 * X * Y + 1 + 4 * n_int
+    E = np.zeros(cap, np.int32)
+    G = np.zeros(cap, np.float64)
+    n = C.c_int(0)
+    lg = np.ascontiguousarray(logG, np.float64)
+    s, e = np.ascontiguousarray(start, np.int32), np.ascontiguousarray(end, np.int32)
+    rc = lib().orc_stitch(ptr(lg), ptr(s), ptr(e), n_int, W, X, Y, ptr(E), ptr(G), cap, C.byref(n), mode)
+    return rc, E[:n.value].copy(), G[:n.value].copy()
 
 
 def reference_run(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W, overlap, alpha, beta, n_iter, xc,

@@ -283,9 +283,26 @@ MainrunOut run_mainrun(const MainrunIn& a, const uint8_t* seen, const int8_t* J,
 
 using Curve = std::map<int, double>;
 
-// result_handling.cpp:115-143.  A shared key without a successor in either
-// map is skipped (the reference dereferences end() there).
-std::tuple<int, double> stitch_key(const Curve& cur, const Curve& nxt)
+// Slope towards the successor key (result_handling.cpp:125-126).  The
+// reference takes std::next of a map's last node too: with libstdc++ that
+// lands on the map header, read as a node whose key is the element count
+// and whose value is the following 8 bytes (~0 in practice).  mode 0
+// (reference) uses that phantom successor (count, 0.0); mode 1 (defined)
+// gives keys without a successor no slope, so they are skipped.
+bool slope_to_next(const Curve& c, Curve::const_iterator a, int mode, double& out)
+{
+  const auto an = std::next(a);
+  if (an != c.end()) {
+    out = (an->second - a->second) / (an->first - a->first);
+    return true;
+  }
+  if (mode != 0) return false;
+  out = (0.0 - a->second) / (static_cast<int>(c.size()) - a->first);
+  return true;
+}
+
+// result_handling.cpp:115-143.
+std::tuple<int, double> stitch_key(const Curve& cur, const Curve& nxt, int mode)
 {
   int best_key = std::numeric_limits<int>::max();
   double best = std::numeric_limits<double>::max();
@@ -293,10 +310,8 @@ std::tuple<int, double> stitch_key(const Curve& cur, const Curve& nxt)
   auto b = nxt.begin();
   while (a != cur.end() && b != nxt.end()) {
     if (a->first == b->first) {
-      const auto an = std::next(a), bn = std::next(b);
-      if (an != cur.end() && bn != nxt.end()) {
-        const double da = (an->second - a->second) / (an->first - a->first);
-        const double db = (bn->second - b->second) / (bn->first - b->first);
+      double da = 0, db = 0;
+      if (slope_to_next(cur, a, mode, da) && slope_to_next(nxt, b, mode, db)) {
         const double d = std::abs(da - db);
         if (d < best) {
           best = d;
@@ -325,7 +340,7 @@ Curve keep_below(const Curve& c, int t, bool below)
 // result_handling.cpp:368-431 (with helpers :26-366).  Returns 0 or a
 // nonzero code when a stitch energy is missing from a window.
 int stitch(const double* logG, const int* start, const int* end, int n_int, int W, int X, int Y,
-           std::vector<std::pair<int, double>>& result)
+           std::vector<std::pair<int, double>>& result, int mode)
 {
   const auto I = static_cast<size_t>(n_int);
   std::vector<Curve> data(I);
@@ -348,7 +363,7 @@ int stitch(const double* logG, const int* start, const int* end, int n_int, int 
     double best = std::numeric_limits<double>::max();
     int best_win = std::numeric_limits<int>::max();
     for (size_t j = i + 1; j < I; ++j) {
-      const auto [key, d] = stitch_key(data[i], data[j]);
+      const auto [key, d] = stitch_key(data[i], data[j], mode);
       if (key < std::numeric_limits<int>::max()) {
         if (d < best) {
           best_key = key;
@@ -480,10 +495,10 @@ int orc_mainrun(int X, int Y, int boundary, int R, int n_int, int W, float overl
 // `logG` is the sample's dense slice (walkers of window 0, then window 1...).
 // Returns 0 and the number of (E, log g) pairs in *n_out, or a nonzero code.
 int orc_stitch(const double* logG, const int* start, const int* end, int n_int, int W, int X, int Y, int* E_out,
-               double* g_out, int cap, int* n_out)
+               double* g_out, int cap, int* n_out, int mode)
 {
   std::vector<std::pair<int, double>> r;
-  const int rc = stitch(logG, start, end, n_int, W, X, Y, r);
+  const int rc = stitch(logG, start, end, n_int, W, X, Y, r, mode);
   if (rc != 0) return rc;
   *n_out = static_cast<int>(r.size());
   if (static_cast<int>(r.size()) > cap) return 3;

@@ -6,6 +6,10 @@
   sources exist; the cubin (device code, git-ignored) travels with the tree.
 * build_harness(): compiles oracle/ref_harness.cu (this project's own driver
   of those kernels) into oracle/_ref/libref_harness.so.
+* build_host(): compiles oracle/ref_host.cpp, which includes the reference's
+  unmodified src/interval.cpp and src/result_handling.cpp where they lie,
+  into oracle/_ref/libref_host.so (host code; only where the reference
+  sources exist, since the x86 library does not travel).
 """
 from __future__ import annotations
 
@@ -16,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(OUT, "wl_ref.cubin")
 HARNESS = os.path.join(OUT, "libref_harness.so")
+HOST = os.path.join(OUT, "libref_host.so")
 REFERENCE = "/root/reference"
 
 
@@ -43,5 +48,21 @@ def build_harness() -> str:
     return HARNESS
 
 
+def build_host() -> str | None:
+    srcs = [os.path.join(REFERENCE, "src", f) for f in ("interval.cpp", "result_handling.cpp")]
+    drv = os.path.join(HERE, "ref_host.cpp")
+    if not all(os.path.exists(f) for f in srcs):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    newest = max(os.path.getmtime(f) for f in srcs + [drv])
+    if os.path.exists(HOST) and os.path.getmtime(HOST) >= newest:
+        return HOST
+    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-Wl,-Bsymbolic-functions",
+                    "-I" + os.path.join(REFERENCE, "src"), "-o", HOST + ".tmp", drv], check=True)
+    os.replace(HOST + ".tmp", HOST)
+    return HOST
+
+
 def build() -> tuple[str | None, str]:
+    build_host()
     return build_cubin(), build_harness()

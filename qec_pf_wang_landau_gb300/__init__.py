@@ -45,6 +45,7 @@ SIGNATURES = {
     "wlg_context_destroy": [P],
     "wlg_context_last_error": [P],
     "wlg_context_set_stream": [P, P],
+    "wlg_context_set_stitching": [P, i32],
     "wlg_solve": [P, P, i32, P, P, P, i64],
     "wlg_solve_couplings": [P, P, i32, P, P, P, P, i64],
     "wlg_frustration": [i32, i32, i32, P, P],
@@ -110,6 +111,9 @@ def couplings_from_syndrome(X: int, Y: int, boundary: int, syndrome):
     J = np.zeros(2 * X * Y, np.int8)
     call("wlg_couplings_from_syndrome", X, Y, boundary, S.ctypes.data_as(P), J.ctypes.data_as(P))
     return J
+
+
+STITCH_REFERENCE, STITCH_DEFINED = 0, 1
 
 
 class WlgError(RuntimeError):
@@ -253,6 +257,10 @@ class Context:
         self._check("wlg_context_set_stream",
                     lib().wlg_context_set_stream(self._h, C.c_void_p(stream) if stream else None))
 
+    def set_stitching(self, mode: int):
+        """STITCH_REFERENCE (default: the reference's output bins) or STITCH_DEFINED for later solves."""
+        self._check("wlg_context_set_stitching", lib().wlg_context_set_stitching(self._h, mode))
+
     def autotune(self, problems, max_outer: int = 2):
         """Time teams-per-CTA choices on `problems` (capped at max_outer outer
         iterations) and keep the fastest per (form, team size) for later solves."""
@@ -315,7 +323,7 @@ def class_log_probs(curves, prob):
 
 class ServerConfig(C.Structure):
     _fields_ = [("mem_budget_bytes", sz), ("epoch_outer", i32), ("max_prerun_batch", i32), ("max_resident", i32),
-                ("fail_after_epochs", i32)]
+                ("fail_after_epochs", i32), ("stitching", i32)]
 
 
 class Decoded(C.Structure):
@@ -334,8 +342,8 @@ class Server:
     poll retired requests with their four class log-probabilities."""
 
     def __init__(self, device: int = 0, mem_budget_bytes: int = 0, epoch_outer: int = 0, max_prerun_batch: int = 0,
-                 max_resident: int = 0, fail_after_epochs: int = 0):
-        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident, fail_after_epochs)
+                 max_resident: int = 0, fail_after_epochs: int = 0, stitching: int = 0):
+        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident, fail_after_epochs, stitching)
         h = C.c_void_p()
         call("wlg_server_create", device, C.byref(cfg), C.byref(h))
         self._h = h

@@ -8,7 +8,8 @@
 // existing result file is extended (it must have been written by this
 // program).  The reference's exchange counter never advances
 // (mainrun.cu:241,346), so by default exchange happens only with -c 1;
-// --exchange-mode 1 exchanges every c iterations.  Exit status: failure when
+// --exchange-mode 1 exchanges every c iterations; --stitching 1 skips
+// energies without a successor where the reference reads past a map's end.  Exit status: failure when
 // a walker finds an energy the pre-run did not (nothing written, as the
 // reference), or on errors.
 
@@ -45,6 +46,7 @@ int main(int argc, char** argv)
     {"task_id", 'd', true, true, "", "Task ID"},
     {"time_limit", 'f', true, true, "", "Time Limit"},
     {"exchange-mode", 0, true, false, "0", "0: as the reference (exchange only with -c 1); 1: every c iterations"},
+    {"stitching", 0, true, false, "0", "0: the reference's output bins; 1: energies without a successor skipped"},
     {"version", 'v', false, false, "", "Show version"},
   });
   try {
@@ -80,6 +82,7 @@ int main(int argc, char** argv)
     const int task = std::stoi(o.str("task_id"));
     const int time_limit = std::stoi(o.str("time_limit"));
     const int xmode = std::stoi(o.str("exchange-mode"));
+    const int stitching = std::stoi(o.str("stitching"));
     if (boundary != 0 && boundary != 1) {
       std::fprintf(stderr, "Unsupported boundary condition %d\n", boundary);
       return EXIT_FAILURE;
@@ -164,6 +167,7 @@ int main(int argc, char** argv)
     std::vector<double> G(static_cast<size_t>(cap));
     wlg_context* ctx = nullptr;
     wlg_status st = wlg_context_create(0, 0, &ctx);
+    if (st == WLG_OK) st = wlg_context_set_stitching(ctx, stitching);
     if (st == WLG_OK)
       st = wlg_mainrun(ctx, probs.data(), R, seen.data(), J.data(), found.data(), energy.data(), lat.data(),
                        static_cast<double>(std::max(time_limit, 0)) + 1e-9,  // -f 0: stop at the first check

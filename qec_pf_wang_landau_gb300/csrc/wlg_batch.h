@@ -29,12 +29,14 @@ wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_
 // ---- windows and stitching (interval.cpp, result_handling.cpp)
 wlg_status make_windows(int e_min, int e_max, int n, float overlap, std::vector<int>& start, std::vector<int>& end);
 using Curve = std::map<int, double>;
-wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<std::pair<int, double>>& out);
+// mode: WLG_STITCH_REFERENCE or WLG_STITCH_DEFINED (wlg_context_set_stitching).
+wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<std::pair<int, double>>& out,
+                          int mode = WLG_STITCH_REFERENCE);
 
 // Stitched, normalised (E, log g) of one finished problem from its compact
 // walker-0 output out[I][L] and its windows win[5 I] (start, end, base, Lb, E0).
 wlg_status stitched_curve(const MainDesc& d, const double* out, const int* win,
-                          std::vector<std::pair<int, double>>& res);
+                          std::vector<std::pair<int, double>>& res, int mode = WLG_STITCH_REFERENCE);
 
 // ---- where a batch runs
 // Device buffers of one batch, by role.

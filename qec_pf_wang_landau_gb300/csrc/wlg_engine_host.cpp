@@ -72,7 +72,26 @@ int energy_host(const int8_t* s, const int8_t* J, int X, int Y, int boundary)
 
 // ----------------------------------------------------------------- stitching --
 
-std::tuple<int, double> best_shared_key(const Curve& a, const Curve& b)
+// Slope of a curve at key x->first towards its successor.  At the curve's
+// last key there is none: the reference (result_handling.cpp:125-126) reads
+// the successor of the map's last node anyway, which with libstdc++ is the
+// map's header, whose key field holds the map's element count and whose
+// value is the next 8 bytes in memory (zero or pointer-sized garbage, ~0 as
+// a double).  Reference mode uses that phantom node (key = count, value 0);
+// defined mode reports "no slope".
+bool slope(const Curve& c, Curve::const_iterator x, int mode, double& out)
+{
+  const auto xn = std::next(x);
+  if (xn != c.end()) {
+    out = (xn->second - x->second) / (xn->first - x->first);
+    return true;
+  }
+  if (mode != WLG_STITCH_REFERENCE) return false;
+  out = (0.0 - x->second) / (static_cast<int>(c.size()) - x->first);
+  return true;
+}
+
+std::tuple<int, double> best_shared_key(const Curve& a, const Curve& b, int mode)
 {
   int key = std::numeric_limits<int>::max();
   double best = std::numeric_limits<double>::max();
@@ -80,10 +99,8 @@ std::tuple<int, double> best_shared_key(const Curve& a, const Curve& b)
   auto y = b.begin();
   while (x != a.end() && y != b.end()) {
     if (x->first == y->first) {
-      const auto xn = std::next(x), yn = std::next(y);
-      if (xn != a.end() && yn != b.end()) {  // keys without a successor have no slope
-        const double dx = (xn->second - x->second) / (xn->first - x->first);
-        const double dy = (yn->second - y->second) / (yn->first - y->first);
+      double dx = 0, dy = 0;
+      if (slope(a, x, mode, dx) && slope(b, y, mode, dy)) {
         const double d = std::abs(dx - dy);
         if (d < best) {
           best = d;
@@ -113,7 +130,7 @@ Curve cut(const Curve& c, int e, bool below)
 
 // result_handling.cpp:368-431.  `windows[b]` holds walker 0's nonzero log g
 // of window b.  Output: normalised (E, log g) pairs, logsumexp = X*Y*ln 2.
-wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<std::pair<int, double>>& out)
+wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<std::pair<int, double>>& out, int mode)
 {
   const size_t I = windows.size();
   for (auto& c : windows) {
@@ -128,7 +145,7 @@ wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<
     double best = std::numeric_limits<double>::max();
     int best_win = -1;
     for (size_t j = i + 1; j < I; ++j) {
-      const auto [key, d] = best_shared_key(windows[i], windows[j]);
+      const auto [key, d] = best_shared_key(windows[i], windows[j], mode);
       if (key == std::numeric_limits<int>::max()) break;
       if (d < best) {
         best = d;
@@ -195,7 +212,7 @@ wlg_status stitch_windows(std::vector<Curve> windows, int X, int Y, std::vector<
 // result_handling.cpp:368-431 applied to the compact walker-0 output of one
 // problem: each window's reachable energies with nonzero log g.
 wlg_status stitched_curve(const MainDesc& d, const double* out, const int* win,
-                          std::vector<std::pair<int, double>>& res)
+                          std::vector<std::pair<int, double>>& res, int mode)
 {
   const int g = 1 << d.lg;
   std::vector<Curve> curves(static_cast<size_t>(d.I));
@@ -206,7 +223,7 @@ wlg_status stitched_curve(const MainDesc& d, const double* out, const int* win,
       if (v != 0) curves[b].emplace(base + c * g, v);
     }
   }
-  return stitch_windows(std::move(curves), d.X, d.Y, res);
+  return stitch_windows(std::move(curves), d.X, d.Y, res, mode);
 }
 
 }  // namespace wlg
@@ -235,6 +252,7 @@ struct wlg_context {
   int launches = 0;
   int main_forms = 0;
   std::map<std::pair<int, int>, int> tuned;  // teams per CTA by (form, team size), from wlg_context_autotune
+  int stitching = WLG_STITCH_REFERENCE;
   std::string err;
 };
 
@@ -853,6 +871,13 @@ wlg_status wlg_context_set_stream(wlg_context* ctx, wlg_stream stream)
   return WLG_OK;
 }
 
+wlg_status wlg_context_set_stitching(wlg_context* ctx, int mode)
+{
+  if (ctx == nullptr || (mode != WLG_STITCH_REFERENCE && mode != WLG_STITCH_DEFINED)) return WLG_ERR_INVALID;
+  ctx->stitching = mode;
+  return WLG_OK;
+}
+
 const char* wlg_context_last_error(const wlg_context* ctx) { return ctx == nullptr ? "" : ctx->err.c_str(); }
 
 wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, wlg_result* results, int* win_start,
@@ -895,7 +920,7 @@ wlg_status stitch_all(wlg_context* ctx, const Prepared& prep, const std::vector<
     for (size_t i = w; i < m; i += workers) {
       if (results[prep.main_problem[i]].status != WLG_OK) continue;
       const MainDesc& d = prep.main[i];
-      sst[i] = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, curves[i]);
+      sst[i] = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, curves[i], ctx->stitching);
     }
   };
   if (workers <= 1) {

@@ -23,7 +23,7 @@
 namespace wlg {
 wlg_status make_windows(int e_min, int e_max, int n, float overlap, std::vector<int>& start, std::vector<int>& end);
 wlg_status stitch_windows(std::vector<std::map<int, double>> windows, int X, int Y,
-                          std::vector<std::pair<int, double>>& out);
+                          std::vector<std::pair<int, double>>& out, int mode);
 }  // namespace wlg
 
 namespace {
@@ -263,7 +263,7 @@ wlg_status run_plain(const wlg_problem& q, int R, cudaStream_t s, std::vector<wl
       for (int e = start[gb]; e <= end[gb]; ++e)
         if (hG[o + e - start[gb]] != 0) wins[b].emplace(e, hG[o + e - start[gb]]);
     }
-    r.status = wlg::stitch_windows(std::move(wins), X, Y, curves[k]);
+    r.status = wlg::stitch_windows(std::move(wins), X, Y, curves[k], WLG_STITCH_REFERENCE);
   }
   return WLG_OK;
 }

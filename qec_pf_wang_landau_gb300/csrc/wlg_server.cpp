@@ -764,7 +764,7 @@ bool wlg_server::retire()
         std::vector<std::pair<int, double>> curve;
         int status = r.status;
         if (status == WLG_OK) {
-          status = stitched_curve(pr.d, outs[i].data(), pr.win.data(), curve);
+          status = stitched_curve(pr.d, outs[i].data(), pr.win.data(), curve, cfg.stitching);
         }
         class_done(pr.req, pr.cls, status, r.outer, std::move(curve));
         reclaim.push_back(s);
@@ -864,6 +864,7 @@ wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_se
     if (s->cfg.max_prerun_batch <= 0) s->cfg.max_prerun_batch = 256;
     if (s->cfg.max_resident <= 0) s->cfg.max_resident = 8192;
     if (s->cfg.max_resident < kClasses) return WLG_ERR_INVALID;
+    if (s->cfg.stitching != WLG_STITCH_REFERENCE && s->cfg.stitching != WLG_STITCH_DEFINED) return WLG_ERR_INVALID;
     s->t0 = Clock::now();
     const wlg_status st = s->setup();
     if (st != WLG_OK) {

@@ -79,22 +79,26 @@ def test_engine_full_run_bit_exact(cuda, cfg):
             assert np.array_equal(wins[b], want), f"sample {k} window {b}: max |d| {np.abs(wins[b] - want).max()}"
     assert total_flips == ref["flips"]
 
-    # stitched result == the oracle's stitching of the same windows
-    solved = ctx.solve(probs)
-    for k, (res, E, G) in enumerate(solved):
-        o = ref["off_hist"][k * I * W]
-        sl = ref["logG"][o:]
-        Eo = np.zeros(4 * X * Y + 1, np.int32)
-        Go = np.zeros(4 * X * Y + 1, np.float64)
-        nout = C.c_int(0)
-        rc = O.lib().orc_stitch(O.ptr(np.ascontiguousarray(sl)), O.ptr(ref["start"][k * I:]),
-                                O.ptr(ref["end"][k * I:]), I, W, X, Y, O.ptr(Eo), O.ptr(Go), len(Eo),
-                                C.byref(nout))
-        assert rc == 0
-        assert np.array_equal(E, Eo[:nout.value])
-        assert np.array_equal(G, Go[:nout.value])
-        lse = np.logaddexp.reduce(G)
-        assert abs(lse - X * Y * np.log(2)) < 1e-9
+    # stitched result == the oracle's stitching of the same windows, in the
+    # reference's mode (the default) and in the defined one
+    for mode in (wlg.STITCH_DEFINED, wlg.STITCH_REFERENCE):
+        ctx.set_stitching(mode)
+        solved = ctx.solve(probs)
+        for k, (res, E, G) in enumerate(solved):
+            o = ref["off_hist"][k * I * W]
+            sl = np.ascontiguousarray(ref["logG"][o:])
+            Eo = np.zeros(4 * X * Y + 1, np.int32)
+            Go = np.zeros(4 * X * Y + 1, np.float64)
+            nout = C.c_int(0)
+            rc = O.lib().orc_stitch(O.ptr(sl), O.ptr(ref["start"][k * I:]), O.ptr(ref["end"][k * I:]), I, W, X, Y,
+                                    O.ptr(Eo), O.ptr(Go), len(Eo), C.byref(nout), mode)
+            if rc != 0:
+                assert res.status == 8, (mode, k, res.status)  # WLG_ERR_STITCH
+                continue
+            assert np.array_equal(E, Eo[:nout.value])
+            assert np.array_equal(G, Go[:nout.value])
+            lse = np.logaddexp.reduce(G)
+            assert abs(lse - X * Y * np.log(2)) < 1e-9
 
 
 # Problems whose per-team state (FP64 + float log g, histogram, lattices) is

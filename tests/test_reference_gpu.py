@@ -21,7 +21,7 @@ def _stitch(windows, starts, ends, X, Y):
     n = C.c_int(0)
     rc = O.lib().orc_stitch(O.ptr(np.ascontiguousarray(flat)), O.ptr(np.ascontiguousarray(starts)),
                             O.ptr(np.ascontiguousarray(ends)), len(windows), W, X, Y, O.ptr(E), O.ptr(G), len(E),
-                            C.byref(n))
+                            C.byref(n), 0)
     assert rc == 0
     return E[:n.value], G[:n.value]
 

@@ -173,3 +173,24 @@ def test_failure_retires_every_request_and_server_stays_usable(cuda):
         assert srv.wait([late], 60)[late].status == 2
         st = srv.stats()
         assert st["completed"] == len(ids) + 1 and st["epochs"] >= 3
+
+
+def test_served_stitching_modes_equal_batch_engine(cuda):
+    """The server's stitching mode is the context's: defined-mode decoding
+    equals the batch engine with WLG_STITCH_DEFINED, bit for bit."""
+    import qec_pf_wang_landau_gb300 as wlg
+    reqs = mixed_requests(wlg, 4)
+    ctx = wlg.Context(0)
+    ctx.set_stitching(wlg.STITCH_DEFINED)
+    with wlg.Server(0, stitching=wlg.STITCH_DEFINED) as srv:
+        ids = srv.submit(reqs)
+        got = srv.wait(ids, 300)
+    for i, q in zip(ids, reqs):
+        statuses, outer, lz, lp = batch_reference(wlg, ctx, q)
+        d = got[i]
+        assert d.status == next((s for s in statuses if s != 0), 0)
+        if d.status == 0:
+            assert list(d.outer_iterations) == outer
+            assert np.array_equal(np.array(d.log_probs), lp)
+    with pytest.raises(wlg.WlgError):
+        wlg.Server(0, stitching=7)
