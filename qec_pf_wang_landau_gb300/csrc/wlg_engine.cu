@@ -292,14 +292,13 @@ __device__ __forceinline__ int energy_after_flip(const Lat& l, uint64_t JR, uint
 
 __device__ __forceinline__ bool mask_has(const uint32_t* mask, int c) { return (mask[c >> 5] >> (c & 31)) & 1u; }
 
-__device__ __forceinline__ uint32_t pick_word(const uint4& A, const uint4& B, int i)  // i in [0, 4]
+// Draws q and q + 1 of the words of A then B (q in [0, 3]); the three
+// compares serve both picks.
+__device__ __forceinline__ void pick_pair(const uint4& A, const uint4& B, int q, uint32_t& x1, uint32_t& x2)
 {
-  uint32_t v = A.x;
-  v = (i == 1) ? A.y : v;
-  v = (i == 2) ? A.z : v;
-  v = (i == 3) ? A.w : v;
-  v = (i == 4) ? B.x : v;
-  return v;
+  const bool q1 = q == 1, q2 = q == 2, q3 = q == 3;
+  x1 = q3 ? A.w : (q2 ? A.z : (q1 ? A.y : A.x));
+  x2 = q3 ? B.x : (q2 ? A.w : (q1 ? A.z : A.y));
 }
 
 // What the walkers of one team share during a sweep.
@@ -355,8 +354,7 @@ struct Walk {
   // after Cb is restarted two steps pass before B runs out and Cb, complete
   // by then, replaces it.
   uint32_t k0, k1, s0, s1, k5a, k5b;
-  uint64_t pos;  // draws consumed
-  uint64_t nc;   // counter of the block being built in Cb
+  uint64_t nc;  // counter of the block being built in Cb (block A's + 2)
   uint4 A, B, Cb;
   int phase;
   int q;  // draw offset in block A, 0..3
@@ -402,7 +400,7 @@ struct Walk {
     k1 = rng.k1;
     s0 = rng.s0;
     s1 = rng.s1;
-    pos = rng.pos;
+    const uint64_t pos = rng.pos;
     const uint64_t blk = pos >> 2;
     A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), s0, s1, k0, k1);
     B = philox10(static_cast<uint32_t>(blk + 1), static_cast<uint32_t>((blk + 1) >> 32), s0, s1, k0, k1);
@@ -421,6 +419,9 @@ struct Walk {
 
   __device__ __forceinline__ bool active(int n_iter) const { return it < n_iter && !stopped; }
 
+  // draws consumed: block A's offset plus q
+  __device__ __forceinline__ uint64_t position() const { return ((nc - 2) << 2) + static_cast<uint64_t>(q); }
+
   __device__ __forceinline__ void step(const SweepCtx& c)
   {
     const MainDesc& d = *c.d;
@@ -431,8 +432,7 @@ struct Walk {
       Cb = phase < 2 ? half : Cb;
       phase = min(phase + 1, 2);
     }
-    x1 = pick_word(A, B, q);
-    x2 = pick_word(A, B, q + 1);
+    pick_pair(A, B, q, x1, x2);
     const float lu = log_uniform(x2);  // depends on the draw only: off the serial path
     // site trunc(u (N - 1 + 0.999999)) (wl.cu:60-66) as floor(x N / 2^32)
     // unless x N lies within site_thr of a multiple of 2^32
@@ -505,7 +505,6 @@ struct Walk {
     h_cur += upd ? 1u : 0u;
     kf += upd ? 1.0f : 0.0f;
     const int used = commit ? (inside ? 2 : 1) : (stop_now ? 1 : 0);  // draws consumed
-    pos += static_cast<uint64_t>(used);
     q += used;
     it += commit ? 1 : 0;
     stopped = stopped || stop_now;
@@ -710,7 +709,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       wa.finish(sc);
       lt = wa.lt;
       E = wa.E;
-      rng.pos = wa.pos;
+      rng.pos = wa.position();
       rng.refill();
     }
     team.sync();
