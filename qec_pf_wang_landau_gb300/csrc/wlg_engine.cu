@@ -301,241 +301,6 @@ __device__ __forceinline__ void pick_pair(const uint4& A, const uint4& B, int q,
   x2 = q3 ? B.x : (q2 ? A.w : (q1 ? A.z : A.y));
 }
 
-// What the walkers of one team share during a sweep.
-struct SweepCtx {
-  const MainDesc* d;
-  int P;
-  double* G;
-  float* Gf;
-  uint32_t* H;
-  const ulonglong2* nbt;
-  const uint32_t* mask;
-  int* misc;
-  uint64_t JR, JD;
-  const uint32_t* Jr_s;
-  const uint32_t* Jd_s;
-  int step_mask, span, Lm1;
-  uint32_t nN;
-};
-
-// One walker's WL sweep (wl.cu:1077-1175).  The step body has no divergent
-// branch: every state update is predicated on `commit`.  The two FP64
-// decisions of the reference that FP32 cannot always settle (a site pick
-// next to a cell boundary, an acceptance inside the FP32 error band) are
-// made in resolve(), called for the lanes that need them from a
-// warp-uniform block after the step, after which those lanes replay the
-// same step (same draws) with the exact answer.  Each walker counts its own
-// steps; the warp loops until all of its walkers are done.  The acceptance
-// draw is peeked and consumed only for in-window proposals, and the Philox
-// block after next is computed speculatively every step.
-template <bool kReg, bool kTable, bool kGlobalG>
-struct Walk {
-  int t;  // walker index in the team (its shared-memory column)
-  bool frozen;
-  double lnf;  // log(f) (wl.cu:1124)
-  float lnf_f;
-  int lo, hi, bb;  // window bounds and base energy
-  Lat lt;
-  int E;
-  int c_cur;
-  double g_cur;
-  // ln f owed to g_cur by the previous step (wl.cu:1124), added one step
-  // late so the FP64 addition overlaps the next step's decision instead of
-  // waiting on a shared-memory load; same additions, same order
-  double owed;
-  Split gbase_split;
-  float ulp_g;
-  float gfb;  // float of g_cur - gbase at the last change of bin
-  float kf;   // ln f increments since then (exact below 2^24)
-  uint32_t h_cur;
-  // Draws: A and B hold the outputs of counters blk and blk + 1; Cb is
-  // Philox of counter blk + 2, advanced five rounds per step (phase 0, 1:
-  // rounds done 0, 5; 2: complete).  A step consumes at most two draws, so
-  // after Cb is restarted two steps pass before B runs out and Cb, complete
-  // by then, replaces it.
-  uint32_t k0, k1, s0, s1, k5a, k5b;
-  uint64_t nc;  // counter of the block being built in Cb (block A's + 2)
-  uint4 A, B, Cb;
-  int phase;
-  int q;  // draw offset in block A, 0..3
-  int it;
-  bool stopped;
-  int ovr_site;  // exact site of the step being replayed
-  int ovr_acc;   // exact acceptance of the step being replayed
-  // the last step's undecided cases, for resolve()
-  uint32_t x1, x2;
-  int c_new;
-  bool need_site, need_acc;
-
-  __device__ __forceinline__ void begin(const SweepCtx& c, int t_, bool frozen_, double lnf_, int lo_, int hi_,
-                                        int bb_, const Lat& lt_, int E_, const Stream& rng)
-  {
-    const MainDesc& d = *c.d;
-    const int P = c.P;
-    t = t_;
-    frozen = frozen_;
-    lnf = lnf_;
-    lnf_f = static_cast<float>(lnf);
-    lo = lo_;
-    hi = hi_;
-    bb = bb_;
-    lt = lt_;
-    E = E_;
-    c_cur = (E - bb) >> d.lg;
-    g_cur = c.G[c_cur * P + t];
-    // float shadows of this walker's log g relative to gbase: differences
-    // inside a window stay small while absolute values reach 1e4, so the
-    // relative shadow keeps the FP32 error bound (and the FP64 fallback
-    // rate) small
-    const double gbase = g_cur;
-    gbase_split = split_float(gbase);
-    for (int cc = 0; cc < d.L; ++cc) c.Gf[cc * P + t] = shadow_split(c.G[cc * P + t], gbase_split);
-    // one rounding of a double of size |g| <= |gbase| + (small shadow terms)
-    ulp_g = static_cast<float>((fabs(gbase) + 1.0) * 0x1p-51);
-    gfb = 0.0f;
-    h_cur = c.H[c_cur * P + t];
-    kf = 0.0f;
-    owed = 0.0;
-    k0 = rng.k0;
-    k1 = rng.k1;
-    s0 = rng.s0;
-    s1 = rng.s1;
-    const uint64_t pos = rng.pos;
-    const uint64_t blk = pos >> 2;
-    A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), s0, s1, k0, k1);
-    B = philox10(static_cast<uint32_t>(blk + 1), static_cast<uint32_t>((blk + 1) >> 32), s0, s1, k0, k1);
-    Cb = philox10(static_cast<uint32_t>(blk + 2), static_cast<uint32_t>((blk + 2) >> 32), s0, s1, k0, k1);
-    phase = 2;
-    k5a = k0 + 5u * kPhiloxWeylA;  // key of round 5
-    k5b = k1 + 5u * kPhiloxWeylB;
-    it = 0;
-    stopped = false;
-    ovr_site = -1;
-    ovr_acc = -1;
-    q = static_cast<int>(pos - (blk << 2));
-    nc = blk + 2;
-    need_site = need_acc = false;
-  }
-
-  __device__ __forceinline__ bool active(int n_iter) const { return it < n_iter && !stopped; }
-
-  // draws consumed: block A's offset plus q
-  __device__ __forceinline__ uint64_t position() const { return ((nc - 2) << 2) + static_cast<uint64_t>(q); }
-
-  __device__ __forceinline__ void step(const SweepCtx& c)
-  {
-    const MainDesc& d = *c.d;
-    const int P = c.P;
-    const bool act = it < d.n_iter && !stopped;
-    {
-      const uint4 half = philox_rounds<5>(Cb, phase == 0 ? k0 : k5a, phase == 0 ? k1 : k5b);
-      Cb = phase < 2 ? half : Cb;
-      phase = min(phase + 1, 2);
-    }
-    pick_pair(A, B, q, x1, x2);
-    const float lu = log_uniform(x2);  // depends on the draw only: off the serial path
-    // site trunc(u (N - 1 + 0.999999)) (wl.cu:60-66) as floor(x N / 2^32)
-    // unless x N lies within site_thr of a multiple of 2^32
-    const uint32_t lo_s = x1 * c.nN;
-    need_site = act && ovr_site < 0 && (lo_s < d.site_thr || lo_s > ~d.site_thr);
-    const int site = ovr_site >= 0 ? ovr_site : static_cast<int>(__umulhi(x1, c.nN));
-    int En;
-    if constexpr (kTable) {
-      const ulonglong2 nt = c.nbt[site];
-      const int unsat = __popcll((lt.r ^ nt.y) & nt.x);
-      const int deg = __popcll(nt.x);
-      const int sb = static_cast<int>((lt.r >> site) & 1ull);
-      En = E + 2 * (1 - 2 * sb) * (deg - 2 * unsat);
-    } else {
-      En = energy_after_flip<kReg>(lt, c.JR, c.JD, c.Jr_s, c.Jd_s, site, E, d);
-    }
-    const int rel = En - d.e_min;
-    const int relc = min(max(rel, 0), c.span);
-    const bool bad = rel != relc || (rel & c.step_mask) != 0 || !mask_has(c.mask, relc >> d.lg);
-    const bool inside = En >= lo && En <= hi;
-    c_new = min(max((En - bb) >> d.lg, 0), c.Lm1);
-    const bool same = c_new == c_cur;
-    const float gfn = c.Gf[c_new * P + t];
-    const uint32_t h_new = c.H[c_new * P + t];
-    const double g_new = kGlobalG ? 0.0 : c.G[c_new * P + t];
-    // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) decided from FP32
-    // values with a proven error bound eps on the exponent; the reference's
-    // FP64 expression decides whenever the bound does not.
-    const float kl = kf * lnf_f;
-    const float df = (gfb - gfn) + kl;
-    // |df - (g_cur - g_new)|: the shadows' relative errors (<= 2^-23) and
-    // the float roundings of kl and df (2^-22 = 2x and 4x them); the k
-    // sequential double additions in g_cur and the double differences, each
-    // <= one rounding at |g| (k + 4 ulp_g); the shadows' absolute error
-    // 2^-44 (g + gbase) each (<= 512 ulp_g for both)
-    const float eps_b = fmaf(0x1p-22f, fabsf(gfb) + kl, (kf + 516.0f) * ulp_g);  // before the load of gfn
-    const float eps = fmaf(0x1p-22f, fabsf(gfn) + fabsf(df), eps_b);
-    const Decision dec = decide(x2, lu, df, eps, same);
-    need_acc = act && !need_site && !bad && inside && ovr_acc < 0 && !dec.known;
-    g_cur += owed;  // g >= +0, so adding +0 (frozen, first step) is exact
-    owed = 0.0;
-    const bool stop_now = act && !need_site && bad;  // wl.cu:1091-1104: a new energy stops the problem
-    if (stop_now) {
-      c.misc[1] = 1;
-      c.misc[2] = En;
-    }
-    const bool commit = act && !need_site && !need_acc && !bad;
-    const bool acc = commit && inside && (ovr_acc >= 0 ? ovr_acc != 0 : dec.acc);
-    flip_spin<kReg>(lt, site, acc);
-    E = acc ? En : E;
-    // leaving c_cur: write back its log g, shadow and visit count
-    const bool chg = acc && !same;
-    const float sh = shadow_split(g_cur, gbase_split);
-    if (chg && !frozen) {
-      c.G[c_cur * P + t] = g_cur;
-      c.Gf[c_cur * P + t] = sh;
-      c.H[c_cur * P + t] = h_cur;
-    }
-    if constexpr (kGlobalG) {
-      if (chg) g_cur = c.G[c_new * P + t];
-    } else {
-      g_cur = chg ? g_new : g_cur;
-    }
-    h_cur = chg ? h_new : h_cur;
-    gfb = chg ? gfn : gfb;
-    kf = chg ? 0.0f : kf;
-    c_cur = chg ? c_new : c_cur;
-    const bool upd = commit && !frozen;
-    owed = upd ? lnf : 0.0;
-    h_cur += upd ? 1u : 0u;
-    kf += upd ? 1.0f : 0.0f;
-    const int used = commit ? (inside ? 2 : 1) : (stop_now ? 1 : 0);  // draws consumed
-    q += used;
-    it += commit ? 1 : 0;
-    stopped = stopped || stop_now;
-    ovr_site = commit || stop_now ? -1 : ovr_site;
-    ovr_acc = commit || stop_now ? -1 : ovr_acc;
-    const bool adv = q >= 4;
-    q = adv ? q - 4 : q;
-    A = adv ? B : A;
-    B = adv ? Cb : B;
-    nc += adv ? 1u : 0u;  // restart Cb on the counter after the new B
-    Cb = adv ? make_uint4(static_cast<uint32_t>(nc), static_cast<uint32_t>(nc >> 32), s0, s1) : Cb;
-    phase = adv ? 0 : phase;
-  }
-
-  // The exact decisions the last step left open (rare).
-  __device__ __forceinline__ void resolve(const SweepCtx& c)
-  {
-    if (need_site) ovr_site = site_exact(x1, c.d->site_scale);
-    if (need_acc) ovr_acc = accept_exact(x2, g_cur, c.G + c_new * c.P + t) ? 1 : 0;
-  }
-
-  __device__ __forceinline__ void finish(const SweepCtx& c)
-  {
-    g_cur += owed;
-    if (!frozen) {
-      c.G[c_cur * c.P + t] = g_cur;
-      c.H[c_cur * c.P + t] = h_cur;
-    }
-  }
-};
-
 template <bool kReg, bool kTable, bool kGlobalG>
 __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base, double* gslot,
                             const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
@@ -651,8 +416,6 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   const int step_mask = (1 << d.lg) - 1;
   const int span = d.e_max - d.e_min;
   const int Lm1 = d.L - 1;
-  const SweepCtx sc{&d, P, G, Gf, H, nbt, mask, misc, JR, JD, Jr_s, Jd_s, step_mask, span, Lm1,
-                    static_cast<uint32_t>(d.N)};
 
   long long outer = 0;
   long long counter = 1;
@@ -693,23 +456,170 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       status = WLG_ERR_TIMEOUT;
       break;
     }
-    // ---- WL sweep (wl.cu:1077-1175), see Walk.
+    // ---- WL sweep (wl.cu:1077-1175).  The step body has no divergent
+    // branch: every state update is predicated on `commit`.  The two FP64
+    // decisions of the reference that FP32 cannot always settle (a site pick
+    // next to a cell boundary, an acceptance inside the FP32 error band) are
+    // made for the few lanes that need them in a warp-uniform block at the
+    // end of the body, after which those lanes replay the same step (same
+    // draws) with the exact answer.  Each lane counts its own steps; the warp
+    // loops until all of its live lanes are done.  The acceptance draw is
+    // peeked and consumed only for in-window proposals, and the Philox block
+    // after next is computed speculatively every step.
     const unsigned wmask = __ballot_sync(0xFFFFFFFFu, live);
     if (live) {
-      Walk<kReg, kTable, kGlobalG> wa;
-      wa.begin(sc, t, cond[b] != 0, lnfw[b], lo, hi, bb, lt, E, rng);
+      const bool frozen = cond[b] != 0;
+      const double lnf = lnfw[b];  // log(f) (wl.cu:1124)
+      const float lnf_f = static_cast<float>(lnf);
+      int c_cur = (E - bb) >> d.lg;
+      double g_cur = G[c_cur * P + t];
+      // float shadows of this walker's log g relative to gbase: differences
+      // inside a window stay small while absolute values reach 1e4, so the
+      // relative shadow keeps the FP32 error bound (and the FP64 fallback
+      // rate) small
+      const double gbase = g_cur;
+      const Split gbase_split = split_float(gbase);
+      for (int c = 0; c < d.L; ++c) Gf[c * P + t] = shadow_split(G[c * P + t], gbase_split);
+      // one rounding of a double of size |g| <= |gbase| + (small shadow terms)
+      const float ulp_g = static_cast<float>((fabs(gbase) + 1.0) * 0x1p-51);
+      float gfb = 0.0f;               // float of g_cur - gbase at the last change of bin
+      uint32_t h_cur = H[c_cur * P + t];
+      float kf = 0.0f;                // ln f increments since then (exact below 2^24)
+      // ln f owed to g_cur by the previous step (wl.cu:1124), added one step
+      // late so the FP64 addition overlaps the next step's decision instead
+      // of waiting on a shared-memory load; same additions, same order
+      double owed = 0.0;
+      // Draws: A and B hold the outputs of counters blk and blk + 1; C is
+      // Philox of counter blk + 2, advanced five rounds per step (phase
+      // 0, 1: rounds done 0, 5; 2: complete).  A step consumes at most two
+      // draws, so after C is restarted two steps pass before B runs out
+      // and C, complete by then, replaces it.
+      const uint64_t pos = rng.pos;
+      const uint64_t blk = pos >> 2;
+      uint4 A = philox10(static_cast<uint32_t>(blk), static_cast<uint32_t>(blk >> 32), rng.s0, rng.s1, rng.k0, rng.k1);
+      uint4 B = philox10(static_cast<uint32_t>(blk + 1), static_cast<uint32_t>((blk + 1) >> 32), rng.s0, rng.s1,
+                         rng.k0, rng.k1);
+      uint4 Cb = philox10(static_cast<uint32_t>(blk + 2), static_cast<uint32_t>((blk + 2) >> 32), rng.s0, rng.s1,
+                          rng.k0, rng.k1);
+      int phase = 2;
+      const uint32_t k5a = rng.k0 + 5u * kPhiloxWeylA, k5b = rng.k1 + 5u * kPhiloxWeylB;  // key of round 5
+      const uint32_t nN = static_cast<uint32_t>(d.N);
+      int it = 0;
+      bool stopped = false;
+      int ovr_site = -1;  // exact site of the step being replayed
+      int ovr_acc = -1;   // exact acceptance of the step being replayed
+      int q = static_cast<int>(pos - (blk << 2));  // draw offset in block A, 0..3
+      uint64_t nc = blk + 2;                        // counter of the block being built in C
       // For the first n_iter warp iterations no live lane has finished (a
       // lane finishes after n_iter committed steps), so the warp votes on
       // continuing only after that, when lanes that replayed catch up.
       for (int k = 0;; ++k) {
-        if (k >= d.n_iter && !__any_sync(wmask, wa.active(d.n_iter))) break;
-        wa.step(sc);
-        if (__any_sync(wmask, wa.need_site || wa.need_acc)) wa.resolve(sc);  // rare
+        const bool act = it < d.n_iter && !stopped;
+        if (k >= d.n_iter && !__any_sync(wmask, act)) break;
+        {
+          const uint4 half = philox_rounds<5>(Cb, phase == 0 ? rng.k0 : k5a, phase == 0 ? rng.k1 : k5b);
+          Cb = phase < 2 ? half : Cb;
+          phase = min(phase + 1, 2);
+        }
+        uint32_t x1, x2;
+        pick_pair(A, B, q, x1, x2);
+        const float lu = log_uniform(x2);  // depends on the draw only: off the serial path
+        // site trunc(u (N - 1 + 0.999999)) (wl.cu:60-66) as floor(x N / 2^32)
+        // unless x N lies within site_thr of a multiple of 2^32
+        const uint32_t lo_s = x1 * nN;
+        const bool need_site = act && ovr_site < 0 && (lo_s < d.site_thr || lo_s > ~d.site_thr);
+        const int site = ovr_site >= 0 ? ovr_site : static_cast<int>(__umulhi(x1, nN));
+        int En;
+        if constexpr (kTable) {
+          const ulonglong2 nt = nbt[site];
+          const int unsat = __popcll((lt.r ^ nt.y) & nt.x);
+          const int deg = __popcll(nt.x);
+          const int sb = static_cast<int>((lt.r >> site) & 1ull);
+          En = E + 2 * (1 - 2 * sb) * (deg - 2 * unsat);
+        } else {
+          En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
+        }
+        const int rel = En - d.e_min;
+        const int relc = min(max(rel, 0), span);
+        const bool bad = rel != relc || (rel & step_mask) != 0 || !mask_has(mask, relc >> d.lg);
+        const bool inside = En >= lo && En <= hi;
+        const int c_new = min(max((En - bb) >> d.lg, 0), Lm1);
+        const bool same = c_new == c_cur;
+        const float gfn = Gf[c_new * P + t];
+        const uint32_t h_new = H[c_new * P + t];
+        const double g_new = kGlobalG ? 0.0 : G[c_new * P + t];
+        // u < min(1, exp(g_cur - g_new)) (wl.cu:1113-1116) decided from FP32
+        // values with a proven error bound eps on the exponent; the
+        // reference's FP64 expression decides whenever the bound does not.
+        const float kl = kf * lnf_f;
+        const float df = (gfb - gfn) + kl;
+        // |df - (g_cur - g_new)|: the shadows' relative errors (<= 2^-23)
+        // and the float roundings of kl and df (2^-22 = 2x and 4x them); the k
+        // sequential double additions in g_cur and the double differences,
+        // each <= one rounding at |g| (k + 4 ulp_g); the shadows' absolute
+        // error 2^-44 (g + gbase) each (<= 512 ulp_g for both)
+        const float eps_b = fmaf(0x1p-22f, fabsf(gfb) + kl, (kf + 516.0f) * ulp_g);  // before the load of gfn
+        const float eps = fmaf(0x1p-22f, fabsf(gfn) + fabsf(df), eps_b);
+        const Decision dec = decide(x2, lu, df, eps, same);
+        const bool fast_acc = dec.acc;
+        const bool known = dec.known;
+        const bool need_acc = act && !need_site && !bad && inside && ovr_acc < 0 && !known;
+        g_cur += owed;  // g >= +0, so adding +0 (frozen, first step) is exact
+        owed = 0.0;
+        const bool stop_now = act && !need_site && bad;  // wl.cu:1091-1104: a new energy stops the problem
+        if (stop_now) {
+          misc[1] = 1;
+          misc[2] = En;
+        }
+        const bool commit = act && !need_site && !need_acc && !bad;
+        const bool acc = commit && inside && (ovr_acc >= 0 ? ovr_acc != 0 : fast_acc);
+        flip_spin<kReg>(lt, site, acc);
+        E = acc ? En : E;
+        // leaving c_cur: write back its log g, shadow and visit count
+        const bool chg = acc && !same;
+        const float sh = shadow_split(g_cur, gbase_split);
+        if (chg && !frozen) {
+          G[c_cur * P + t] = g_cur;
+          Gf[c_cur * P + t] = sh;
+          H[c_cur * P + t] = h_cur;
+        }
+        if constexpr (kGlobalG) {
+          if (chg) g_cur = G[c_new * P + t];
+        } else {
+          g_cur = chg ? g_new : g_cur;
+        }
+        h_cur = chg ? h_new : h_cur;
+        gfb = chg ? gfn : gfb;
+        kf = chg ? 0.0f : kf;
+        c_cur = chg ? c_new : c_cur;
+        const bool upd = commit && !frozen;
+        owed = upd ? lnf : 0.0;
+        h_cur += upd ? 1u : 0u;
+        kf += upd ? 1.0f : 0.0f;
+        const int used = commit ? (inside ? 2 : 1) : (stop_now ? 1 : 0);  // draws consumed
+        q += used;
+        it += commit ? 1 : 0;
+        stopped = stopped || stop_now;
+        ovr_site = commit || stop_now ? -1 : ovr_site;
+        ovr_acc = commit || stop_now ? -1 : ovr_acc;
+        const bool adv = q >= 4;
+        q = adv ? q - 4 : q;
+        A = adv ? B : A;
+        B = adv ? Cb : B;
+        nc += adv ? 1u : 0u;  // restart C on the counter after the new B
+        Cb = adv ? make_uint4(static_cast<uint32_t>(nc), static_cast<uint32_t>(nc >> 32), rng.s0, rng.s1) : Cb;
+        phase = adv ? 0 : phase;
+        if (__any_sync(wmask, need_site || need_acc)) {  // rare
+          if (need_site) ovr_site = site_exact(x1, d.site_scale);
+          if (need_acc) ovr_acc = accept_exact(x2, g_cur, G + c_new * P + t) ? 1 : 0;
+        }
       }
-      wa.finish(sc);
-      lt = wa.lt;
-      E = wa.E;
-      rng.pos = wa.position();
+      g_cur += owed;
+      if (!frozen) {
+        G[c_cur * P + t] = g_cur;
+        H[c_cur * P + t] = h_cur;
+      }
+      rng.pos = ((nc - 2) << 2) + static_cast<uint64_t>(q);  // draws consumed: block A's offset plus q
       rng.refill();
     }
     team.sync();
