@@ -13,6 +13,7 @@
 
 #include "../../include/wlg.h"
 #include "wlg_engine.h"
+#include "wlg_pool.h"
 
 namespace wlg {
 
@@ -75,6 +76,7 @@ struct Exec {
   // teams per CTA chosen by an autotuner, by (form, team size); nullptr or
   // no entry: the built-in rule
   const std::map<std::pair<int, int>, int>* per_cta = nullptr;
+  WorkerPool* pool = nullptr;  // host threads for the per-problem phases; nullptr: the calling thread
   virtual ~Exec() = default;
   // device buffer for `slot` of at least `bytes` bytes
   virtual wlg_status buffer(Slot slot, size_t bytes, void** out) = 0;
@@ -114,7 +116,7 @@ struct Prepared {
   std::vector<MainDesc> main;                  // problems that reach the main run
   std::vector<int> main_problem;               // index into the batch
   std::vector<std::vector<int>> starts, ends;  // per batch problem
-  std::vector<int> lg, base_off;               // per main entry: log2 step, offset of w_base in win pool
+  std::vector<int> lg;                         // per main entry: log2 of the energy step
 };
 
 // Main-run inputs of a prepared batch, on the host: packed couplings, start

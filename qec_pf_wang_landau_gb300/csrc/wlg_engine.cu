@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ 
       int site = static_cast<int>(__umulhi(xs, static_cast<uint32_t>(N)));
       if (lo_s < site_thr || lo_s > ~site_thr)
         site = static_cast<int>(trunc(static_cast<double>(unit_float(xs)) * site_scale));
-      const Move m = move_i8(s, J, energy, X, Y, site, d.boundary);
+      const Move m = move_i8(s, J, energy, X, Y, site, d.boundary, d.site_magic);
       const int io = energy - e_min;
       const int in = m.new_energy - e_min;
       const long long dd = static_cast<long long>(hist[io]) - static_cast<long long>(hist[in]);
@@ -156,7 +156,16 @@ __global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ 
     }
     __syncthreads();
     int bin = -1;
-    if (hit >= 0) atomicAdd(&hist[hit], 1ull);
+    {
+      // warp-aggregated histogram update: walkers sit on few energies (all
+      // start on one), so lanes with the same bin add their count once
+      const unsigned on = __ballot_sync(0xFFFFFFFFu, hit >= 0);
+      if (hit >= 0) {
+        const unsigned same = __match_any_sync(on, hit);
+        if (static_cast<int>(threadIdx.x & 31u) == __ffs(same) - 1)
+          atomicAdd(&hist[hit], static_cast<unsigned long long>(__popc(same)));
+      }
+    }
     if (acc) {
       const int q = (energy - e_min) / d.len_int;
       bin = (q < d.n_int) ? q : d.n_int - 1;

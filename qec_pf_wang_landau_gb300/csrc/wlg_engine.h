@@ -29,6 +29,7 @@ struct PreDesc {
   int len_int;      // coarse bin width (interval.cpp with overlap 1)
   int n_iter;
   int given_J;          // 1: the class-'i' couplings are read from off_J instead of drawn
+  uint32_t site_magic;  // ceil(2^20 / Y) when it divides every site exactly, else 0
   long long off_J;      // int8 [2N]
   long long off_seen;   // uint8 [4N+1]
   long long off_found;  // int8 [n_int][N]

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
 #include <numbers>
 #include <string>
 #include <thread>
@@ -23,6 +24,7 @@
 #include "wlg_engine.h"
 #include "wlg_internal.h"
 #include "wlg_keys.h"
+#include "wlg_pool.h"
 
 namespace wlg {
 
@@ -254,6 +256,13 @@ struct wlg_context {
   std::map<std::pair<int, int>, int> tuned;  // teams per CTA by (form, team size), from wlg_context_autotune
   int stitching = WLG_STITCH_REFERENCE;
   std::string err;
+  std::unique_ptr<wlg::WorkerPool> pool;  // host threads of the per-problem phases, started on first use
+  wlg::WorkerPool& workers()
+  {
+    if (!pool) pool = std::make_unique<wlg::WorkerPool>(
+      static_cast<int>(std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+    return *pool;
+  }
 };
 
 namespace {
@@ -291,6 +300,7 @@ struct ContextExec final : Exec {
     stream = c->stream;
     ev = c->ev;
     per_cta = &c->tuned;
+    pool = &c->workers();
   }
   wlg_status buffer(Slot slot, size_t bytes, void** out) override
   {
@@ -356,6 +366,9 @@ wlg_status prerun_descs(const wlg_problem* probs, int n, wlg_result* results, Pr
     }
     d.len_int = e[0] - s[0] + 1;
     d.n_iter = q.pre_iterations;
+    d.site_magic = static_cast<uint32_t>(((1u << 20) + q.Y - 1) / q.Y);
+    for (int site = 0; site < d.N && d.site_magic != 0; ++site)
+      if (static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20) != site / q.Y) d.site_magic = 0;
     d.off_J = oJ;
     d.off_seen = oS;
     d.off_found = oF;
@@ -438,16 +451,182 @@ wlg_status run_prerun(Exec& ex, const wlg_problem* probs, int n, wlg_result* res
 
 // The hand-off to the main run (file_io.cpp:558-659, mainrun.cu:79-113)
 // from pre-run outputs.
+namespace {
+
+// One problem's share of the hand-off, computed independently of the others.
+struct HandoffPart {
+  wlg_status status = WLG_OK;  // the problem's own failure (no lattice, windows)
+  wlg_status fatal = WLG_OK;   // a failure of the whole batch
+  const char* why = "";
+  bool windows = false;  // ws/we were made
+  bool main = false;     // the problem reaches the main run
+  MainDesc d{};
+  int lg = 0;
+  std::vector<int> ws, we, win;
+  std::vector<uint32_t> Jw, latw, maskw;
+};
+
+void handoff_one(const wlg_problem& q, const PreDesc& a, const PreOut& po, HandoffPart& out)
+{
+  const std::vector<int8_t>& J8 = po.J8;
+  const std::vector<int8_t>& found = po.found;
+  const std::vector<int>& fflag = po.fflag;
+  const int N = a.N;
+  const uint8_t* h = po.seen.data() + a.off_seen;
+  int first = -1, last = -1;
+  for (int i = 0; i <= 4 * N; ++i)
+    if (h[i] == 1) {
+      if (first < 0) first = i;
+      last = i;
+    }
+  if (first < 0) {
+    out.status = WLG_ERR_NO_LATTICE;
+    return;
+  }
+  const int e_lo = -2 * N + first, e_hi = -2 * N + last;
+  std::vector<int>& ws = out.ws;
+  std::vector<int>& we = out.we;
+  const wlg_status wst = wlg::make_windows(e_lo, e_hi, q.intervals, q.overlap, ws, we);
+  if (wst != WLG_OK) {
+    out.status = wst;
+    return;
+  }
+  out.windows = true;
+  // energy step of the lattice: 4 when every site has an even number of
+  // bonds (periodic, or open 2x2), else 2; checked against the spectrum
+  int g = (q.boundary == 0 || (q.X == 2 && q.Y == 2)) ? 4 : 2;
+  for (int i = first; i <= last; ++i)
+    if (h[i] == 1 && (i - first) % g != 0) g = ((i - first) % 2 == 0) ? 2 : 1;
+  const int lg = g == 4 ? 2 : (g == 2 ? 1 : 0);
+  // start lattices: lowest-energy stored lattice inside each window
+  std::map<int, int> by_energy;
+  for (int k = 0; k < a.n_int; ++k)
+    if (fflag[a.off_fflag + k] != 0) by_energy.emplace(fflag[a.off_fflag + a.n_int + k], k);
+  const int nwL = (N + 31) / 32;
+  std::vector<int> pick(static_cast<size_t>(q.intervals), -1), E0(static_cast<size_t>(q.intervals));
+  bool ok = true;
+  for (int b = 0; b < q.intervals && ok; ++b) {
+    for (const auto& [en, k] : by_energy)
+      if (en >= ws[b] && en <= we[b]) {
+        pick[b] = k;
+        E0[b] = en;
+        break;
+      }
+    ok = pick[b] >= 0;
+  }
+  if (!ok) {
+    out.status = WLG_ERR_NO_LATTICE;
+    return;
+  }
+  MainDesc& d = out.d;
+  d.X = q.X;
+  d.Y = q.Y;
+  d.N = N;
+  d.boundary = q.boundary;
+  d.I = q.intervals;
+  d.W = q.walkers_per_interval;
+  d.nwalk = d.I * d.W;
+  d.team = round32(d.nwalk);
+  d.e_min = e_lo;
+  d.e_max = e_hi;
+  d.lg = lg;
+  d.n_iter = q.iterations;
+  d.exch_every = q.exchange_every;
+  d.exch_mode = q.exchange_mode;
+  d.parity_base = q.global_parity ? static_cast<int>((static_cast<long long>(q.sample) * q.intervals) & 1) : 0;
+  d.alpha = q.alpha;
+  d.beta = q.beta;
+  d.loop_lim = std::exp(q.beta);
+  d.key_wl = static_cast<uint32_t>(wlg::key_u32(q.seed, static_cast<uint64_t>(q.sample)));
+  d.key_ex = wlg::key_i32(q.seed, static_cast<uint64_t>(q.sample));
+  d.site_magic = static_cast<uint32_t>(((1u << 20) + q.Y - 1) / q.Y);
+  for (int site = 0; site < N; ++site)
+    if (static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20) != site / q.Y) ok = false;
+  if (!ok) {
+    out.fatal = WLG_ERR_INVALID;
+    out.why = "lattice too large for the site division";
+    return;
+  }
+  d.site_scale = (N - 1 + 0.999999);
+  d.site_thr = static_cast<uint32_t>(N) * 2048u + 16384u;
+  d.max_outer = q.max_outer;
+  d.nwL = nwL;
+  const int nbins = (e_hi - e_lo) / g + 1;
+  d.nwM = (nbins + 31) / 32;
+  // windows: start, end, compact base (first energy >= start on the lattice
+  // of reachable energies), compact length, start energy
+  int L = 1;
+  std::vector<int> base(static_cast<size_t>(d.I)), len(static_cast<size_t>(d.I));
+  for (int b = 0; b < d.I; ++b) {
+    const int r = ((e_lo - ws[b]) % g + g) % g;
+    base[b] = ws[b] + r;
+    len[b] = base[b] <= we[b] ? (we[b] - base[b]) / g + 1 : 0;
+    L = std::max(L, len[b]);
+  }
+  d.L = L;
+  for (int half = 0; half < 2; ++half)
+    for (int wd = 0; wd < nwL; ++wd) {
+      uint32_t v = 0;
+      for (int bit = 0; bit < 32; ++bit) {
+        const int q2 = wd * 32 + bit;
+        if (q2 < N && J8[a.off_J + half * N + q2] == -1) v |= 1u << bit;
+      }
+      out.Jw.push_back(v);
+    }
+  for (int b = 0; b < d.I; ++b) {
+    const int8_t* src = found.data() + a.off_found + static_cast<long long>(pick[b]) * N;
+    if (wlg::energy_host(src, J8.data() + a.off_J, q.X, q.Y, q.boundary) != E0[b]) {
+      out.fatal = WLG_ERR_ENERGY_RANGE;
+      out.why = "stored lattice energy mismatch";
+      return;
+    }
+    for (int wd = 0; wd < nwL; ++wd) {
+      uint32_t v = 0;
+      for (int bit = 0; bit < 32; ++bit) {
+        const int q2 = wd * 32 + bit;
+        if (q2 < N && src[q2] == -1) v |= 1u << bit;
+      }
+      out.latw.push_back(v);
+    }
+  }
+  std::vector<int>& win = out.win;
+  win.insert(win.end(), ws.begin(), ws.end());
+  win.insert(win.end(), we.begin(), we.end());
+  win.insert(win.end(), base.begin(), base.end());
+  win.insert(win.end(), len.begin(), len.end());
+  win.insert(win.end(), E0.begin(), E0.end());
+  for (int wd = 0; wd < d.nwM; ++wd) {
+    uint32_t v = 0;
+    for (int bit = 0; bit < 32; ++bit) {
+      const int c = wd * 32 + bit;
+      if (c < nbins && h[first + c * g] == 1) v |= 1u << bit;
+    }
+    out.maskw.push_back(v);
+  }
+  d.off_state = -1;
+  d.epoch_outer = 0;
+  out.lg = lg;
+  out.main = true;
+}
+
+}  // namespace
+
 wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, const PreOut& po, Prepared& prep,
                    Handoff& ho)
 {
   using clock = std::chrono::steady_clock;
-  const std::vector<PreDesc>& pd = po.pd;
-  const std::vector<int8_t>& J8 = po.J8;
-  const std::vector<int8_t>& found = po.found;
-  const std::vector<uint8_t>& seen = po.seen;
-  const std::vector<int>& fflag = po.fflag;
   const auto t0 = clock::now();
+  // problems are independent: the host workers take them in chunks, then
+  // the parts are packed in problem order
+  std::vector<HandoffPart> parts(static_cast<size_t>(n));
+  const auto one = [&](int p) { handoff_one(probs[p], po.pd[p], po, parts[p]); };
+  if (ex.pool != nullptr) {
+    ex.pool->run(n, 8, one);
+  } else {
+    for (int p = 0; p < n; ++p) one(p);
+  }
+  for (const HandoffPart& part : parts)
+    if (part.fatal != WLG_OK) return fail(ex, part.fatal, part.why);
   std::vector<uint32_t>& Jw = ho.Jw;
   std::vector<uint32_t>& latw = ho.latw;
   std::vector<uint32_t>& maskw = ho.maskw;
@@ -460,143 +639,30 @@ wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* result
   prep.starts.assign(static_cast<size_t>(n), {});
   prep.ends.assign(static_cast<size_t>(n), {});
   for (int p = 0; p < n; ++p) {
-    const wlg_problem& q = probs[p];
-    const PreDesc& a = pd[p];
-    const int N = a.N;
-    const uint8_t* h = seen.data() + a.off_seen;
-    int first = -1, last = -1;
-    for (int i = 0; i <= 4 * N; ++i)
-      if (h[i] == 1) {
-        if (first < 0) first = i;
-        last = i;
-      }
-    if (first < 0) {
-      results[p].status = WLG_ERR_NO_LATTICE;
+    HandoffPart& part = parts[p];
+    if (part.windows) {
+      prep.starts[p] = std::move(part.ws);
+      prep.ends[p] = std::move(part.we);
+    }
+    if (part.status != WLG_OK) {
+      results[p].status = part.status;
       continue;
     }
-    const int e_lo = -2 * N + first, e_hi = -2 * N + last;
-    std::vector<int> ws, we;
-    const wlg_status wst = wlg::make_windows(e_lo, e_hi, q.intervals, q.overlap, ws, we);
-    if (wst != WLG_OK) {
-      results[p].status = wst;
-      continue;
-    }
-    prep.starts[p] = ws;
-    prep.ends[p] = we;
-    // energy step of the lattice: 4 when every site has an even number of
-    // bonds (periodic, or open 2x2), else 2; checked against the spectrum
-    int g = (q.boundary == 0 || (q.X == 2 && q.Y == 2)) ? 4 : 2;
-    for (int i = first; i <= last; ++i)
-      if (h[i] == 1 && (i - first) % g != 0) g = ((i - first) % 2 == 0) ? 2 : 1;
-    const int lg = g == 4 ? 2 : (g == 2 ? 1 : 0);
-    // start lattices: lowest-energy stored lattice inside each window
-    std::map<int, int> by_energy;
-    for (int k = 0; k < a.n_int; ++k)
-      if (fflag[a.off_fflag + k] != 0) by_energy.emplace(fflag[a.off_fflag + a.n_int + k], k);
-    const int nwL = (N + 31) / 32;
-    std::vector<int> pick(static_cast<size_t>(q.intervals), -1), E0(static_cast<size_t>(q.intervals));
-    bool ok = true;
-    for (int b = 0; b < q.intervals && ok; ++b) {
-      for (const auto& [en, k] : by_energy)
-        if (en >= ws[b] && en <= we[b]) {
-          pick[b] = k;
-          E0[b] = en;
-          break;
-        }
-      ok = pick[b] >= 0;
-    }
-    if (!ok) {
-      results[p].status = WLG_ERR_NO_LATTICE;
-      continue;
-    }
-    MainDesc d{};
-    d.X = q.X;
-    d.Y = q.Y;
-    d.N = N;
-    d.boundary = q.boundary;
-    d.I = q.intervals;
-    d.W = q.walkers_per_interval;
-    d.nwalk = d.I * d.W;
-    d.team = round32(d.nwalk);
-    d.e_min = e_lo;
-    d.e_max = e_hi;
-    d.lg = lg;
-    d.n_iter = q.iterations;
-    d.exch_every = q.exchange_every;
-    d.exch_mode = q.exchange_mode;
-    d.parity_base = q.global_parity ? static_cast<int>((static_cast<long long>(q.sample) * q.intervals) & 1) : 0;
-    d.alpha = q.alpha;
-    d.beta = q.beta;
-    d.loop_lim = std::exp(q.beta);
-    d.key_wl = static_cast<uint32_t>(wlg::key_u32(q.seed, static_cast<uint64_t>(q.sample)));
-    d.key_ex = wlg::key_i32(q.seed, static_cast<uint64_t>(q.sample));
-    d.site_magic = static_cast<uint32_t>(((1u << 20) + q.Y - 1) / q.Y);
-    for (int site = 0; site < N; ++site)
-      if (static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20) != site / q.Y) ok = false;
-    if (!ok) return fail(ex, WLG_ERR_INVALID, "lattice too large for the site division");
-    d.site_scale = (N - 1 + 0.999999);
-    d.site_thr = static_cast<uint32_t>(N) * 2048u + 16384u;
-    d.max_outer = q.max_outer;
-    d.nwL = nwL;
-    const int nbins = (e_hi - e_lo) / g + 1;
-    d.nwM = (nbins + 31) / 32;
-    // windows: start, end, compact base (first energy >= start on the lattice
-    // of reachable energies), compact length, start energy
-    int L = 1;
-    std::vector<int> base(static_cast<size_t>(d.I)), len(static_cast<size_t>(d.I));
-    for (int b = 0; b < d.I; ++b) {
-      const int r = ((e_lo - ws[b]) % g + g) % g;
-      base[b] = ws[b] + r;
-      len[b] = base[b] <= we[b] ? (we[b] - base[b]) / g + 1 : 0;
-      L = std::max(L, len[b]);
-    }
-    d.L = L;
+    if (!part.main) continue;
+    MainDesc d = part.d;
     d.off_J = static_cast<long long>(Jw.size());
-    for (int half = 0; half < 2; ++half)
-      for (int wd = 0; wd < nwL; ++wd) {
-        uint32_t v = 0;
-        for (int bit = 0; bit < 32; ++bit) {
-          const int q2 = wd * 32 + bit;
-          if (q2 < N && J8[a.off_J + half * N + q2] == -1) v |= 1u << bit;
-        }
-        Jw.push_back(v);
-      }
+    Jw.insert(Jw.end(), part.Jw.begin(), part.Jw.end());
     d.off_lat = static_cast<long long>(latw.size());
-    for (int b = 0; b < d.I; ++b) {
-      const int8_t* src = found.data() + a.off_found + static_cast<long long>(pick[b]) * N;
-      if (wlg::energy_host(src, J8.data() + a.off_J, q.X, q.Y, q.boundary) != E0[b])
-        return fail(ex, WLG_ERR_ENERGY_RANGE, "stored lattice energy mismatch");
-      for (int wd = 0; wd < nwL; ++wd) {
-        uint32_t v = 0;
-        for (int bit = 0; bit < 32; ++bit) {
-          const int q2 = wd * 32 + bit;
-          if (q2 < N && src[q2] == -1) v |= 1u << bit;
-        }
-        latw.push_back(v);
-      }
-    }
+    latw.insert(latw.end(), part.latw.begin(), part.latw.end());
     d.off_win = static_cast<long long>(win.size());
-    win.insert(win.end(), ws.begin(), ws.end());
-    win.insert(win.end(), we.begin(), we.end());
-    win.insert(win.end(), base.begin(), base.end());
-    win.insert(win.end(), len.begin(), len.end());
-    win.insert(win.end(), E0.begin(), E0.end());
+    win.insert(win.end(), part.win.begin(), part.win.end());
     d.off_mask = static_cast<long long>(maskw.size());
-    for (int wd = 0; wd < d.nwM; ++wd) {
-      uint32_t v = 0;
-      for (int bit = 0; bit < 32; ++bit) {
-        const int c = wd * 32 + bit;
-        if (c < nbins && h[first + c * g] == 1) v |= 1u << bit;
-      }
-      maskw.push_back(v);
-    }
+    maskw.insert(maskw.end(), part.maskw.begin(), part.maskw.end());
     d.off_out = o_out;
     o_out += static_cast<long long>(d.I) * d.L;
-    d.off_state = -1;
-    d.epoch_outer = 0;
     prep.main.push_back(d);
     prep.main_problem.push_back(p);
-    prep.lg.push_back(lg);
+    prep.lg.push_back(part.lg);
   }
   ex.t_handoff = std::chrono::duration<double, std::milli>(clock::now() - t0).count();
   ho.n_out = o_out;
@@ -914,22 +980,11 @@ wlg_status stitch_all(wlg_context* ctx, const Prepared& prep, const std::vector<
   // problem order
   std::vector<std::vector<std::pair<int, double>>> curves(m);
   std::vector<wlg_status> sst(m, WLG_OK);
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const size_t workers = std::min<size_t>({static_cast<size_t>(hw), 16, (m + 31) / 32});
-  auto work = [&](size_t w) {
-    for (size_t i = w; i < m; i += workers) {
-      if (results[prep.main_problem[i]].status != WLG_OK) continue;
-      const MainDesc& d = prep.main[i];
-      sst[i] = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, curves[i], ctx->stitching);
-    }
-  };
-  if (workers <= 1) {
-    work(0);
-  } else {
-    std::vector<std::thread> pool;
-    for (size_t w = 0; w < workers; ++w) pool.emplace_back(work, w);
-    for (std::thread& th : pool) th.join();
-  }
+  ctx->workers().run(static_cast<int>(m), 8, [&](int i) {
+    if (results[prep.main_problem[i]].status != WLG_OK) return;
+    const MainDesc& d = prep.main[i];
+    sst[i] = wlg::stitched_curve(d, out.data() + d.off_out, win.data() + d.off_win, curves[i], ctx->stitching);
+  });
   long long pos = 0;
   for (size_t i = 0; i < m; ++i) {
     wlg_result& r = results[prep.main_problem[i]];

@@ -18,11 +18,13 @@ struct Move {
 // that would wrap.  Couplings: right bond of (i,j) at i*Y+j, down bond at
 // N+i*Y+j.
 // Energy after flipping `site` of the int8 lattice s (wl.cu:52-156).
+// magic: ceil(2^20 / Y) when site * magic >> 20 == site / Y for every site
+// (checked by the caller), 0 to divide.
 __device__ __forceinline__ Move move_i8(const int8_t* __restrict__ s, const int8_t* __restrict__ J, int E, int X,
-                                        int Y, int site, int boundary)
+                                        int Y, int site, int boundary, uint32_t magic = 0)
 {
   const int N = X * Y;
-  const int i = site / Y;
+  const int i = magic != 0 ? static_cast<int>((static_cast<uint32_t>(site) * magic) >> 20) : site / Y;
   const int j = site - i * Y;
   const int ip = (i + 1 < X) ? i + 1 : 0;
   const int im = (i - 1 >= 0) ? i - 1 : X - 1;

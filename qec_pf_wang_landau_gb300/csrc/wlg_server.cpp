@@ -277,6 +277,7 @@ struct wlg_server {
   std::vector<cudaEvent_t> admit_ev;
   std::vector<int> reclaim;  // finished slots waiting for their epochs
   std::unique_ptr<GrowExec> pre;  // used by the admission thread only
+  std::unique_ptr<WorkerPool> apool;  // host workers of the admission's hand-off
   int sms = 1;
 
   // admission thread: pre-run + hand-off of one job at a time
@@ -326,6 +327,8 @@ wlg_status wlg_server::setup()
   pre = std::make_unique<GrowExec>();
   pre->device = device;
   pre->stream = s_pre;
+  apool = std::make_unique<WorkerPool>(static_cast<int>(std::min(8u, std::max(1u, std::thread::hardware_concurrency()))));
+  pre->pool = apool.get();
   stats.bytes_budget = static_cast<long long>(cfg.mem_budget_bytes);
   return WLG_OK;
 }
@@ -350,6 +353,7 @@ void wlg_server::teardown()
   for (cudaEvent_t e : admit_ev) cudaEventDestroy(e);
   admit_ev.clear();
   pre.reset();
+  apool.reset();
   cudaFree(d_desc);
   cudaFree(d_res);
   cudaFree(arena_dev);
