@@ -45,6 +45,8 @@ constexpr double kE = 2.718281828459045;  // std::numbers::e, mainrun.cu:56
 
 // ------------------------------------------------------------ pre-run -----
 
+__device__ __noinline__ int site_exact(uint32_t x, double scale);
+
 __global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ descs, int n,
                                                     int8_t* __restrict__ Jpool, uint8_t* __restrict__ seen_pool,
                                                     int8_t* __restrict__ found_pool, int* __restrict__ fflag_pool)
@@ -138,21 +140,17 @@ __global__ void __launch_bounds__(1024) k_pre_batch(const PreDesc* __restrict__ 
       const uint32_t xs = rng.raw();
       const uint32_t lo_s = xs * static_cast<uint32_t>(N);
       int site = static_cast<int>(__umulhi(xs, static_cast<uint32_t>(N)));
-      if (lo_s < site_thr || lo_s > ~site_thr)
-        site = static_cast<int>(trunc(static_cast<double>(unit_float(xs)) * site_scale));
+      if (lo_s < site_thr || lo_s > ~site_thr) site = site_exact(xs, site_scale);  // out of line: FP64
       const Move m = move_i8(s, J, energy, X, Y, site, d.boundary, d.site_magic);
       const int io = energy - e_min;
       const int in = m.new_energy - e_min;
       const long long dd = static_cast<long long>(hist[io]) - static_cast<long long>(hist[in]);
       const uint32_t xa = rng.raw();
-      if (dd >= 1 || (dd >= -24 && xa < acc_thr[-dd])) {
-        s[m.site] = static_cast<int8_t>(-s[m.site]);
-        energy = m.new_energy;
-        acc = true;
-        hit = in;
-      } else {
-        hit = io;
-      }
+      const int ti = static_cast<int>(min(max(-dd, 0ll), 24ll));
+      acc = dd >= 1 || (dd >= -24 && xa < acc_thr[ti]);
+      if (acc) s[m.site] = static_cast<int8_t>(-s[m.site]);
+      energy = acc ? m.new_energy : energy;
+      hit = acc ? in : io;
     }
     __syncthreads();
     int bin = -1;
