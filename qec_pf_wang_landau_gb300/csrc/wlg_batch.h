@@ -77,6 +77,12 @@ struct Exec {
   // no entry: the built-in rule
   const std::map<std::pair<int, int>, int>* per_cta = nullptr;
   WorkerPool* pool = nullptr;  // host threads for the per-problem phases; nullptr: the calling thread
+  // streams on which the main-run launches of different groups run side by
+  // side (fork/join through aux_ev: [0] fork, [1 + a] join of aux[a]);
+  // n_aux = 0: all on `stream`, one after another
+  cudaStream_t* aux = nullptr;
+  cudaEvent_t* aux_ev = nullptr;
+  int n_aux = 0;
   virtual ~Exec() = default;
   // device buffer for `slot` of at least `bytes` bytes
   virtual wlg_status buffer(Slot slot, size_t bytes, void** out) = 0;
@@ -156,18 +162,30 @@ wlg_status handoff(Exec& ex, const wlg_problem* probs, int n, wlg_result* result
 wlg_status prepare_batch(Exec& ex, const wlg_problem* probs, int n, wlg_result* results, Prepared& prep, Handoff& ho,
                          const int8_t* couplings = nullptr, const unsigned char* given = nullptr);
 
-// Main-run form of a problem by lattice storage: 0 spins in shared memory,
-// 1 spins in a register, 2 register spins + neighbour table (X, Y >= 3);
-// form 3 (FP64 log g in global memory) replaces 0 when the team's state
-// exceeds shared memory.
+// Main-run forms by lattice storage: 0 spins in shared memory, 1 spins in a
+// register, 2 register spins + neighbour table (X, Y >= 3), 3 as 0 with
+// FP64 log g in global memory (teams whose state exceeds shared memory).
+// (Spins of 65-256-site lattices in 2-4 register words with a neighbour
+// table were built and measured: 3-7 % slower than form 0, whose loads are
+// broadcasts or conflict-free columns.)
+constexpr int kSmemBytes = 227 * 1024;
+
 inline int main_form(const MainDesc& d) { return d.N > 64 ? 0 : (d.X >= 3 && d.Y >= 3 ? 2 : 1); }
 
 // Shared-memory bytes of a team running d in form `form`.
 inline int team_bytes(const MainDesc& d, int form, int team)
 {
-  return align16(team_layout(team, d.L, d.nwL, d.nwM, d.I, form == 1 || form == 2, form == 2 ? d.N : 0, form != 3)
-                     .bytes +
+  const bool reg = form == 1 || form == 2;
+  return align16(team_layout(team, d.L, d.nwL, d.nwM, d.I, reg ? 2 : d.nwL, form == 2 ? d.N : 0, form != 3).bytes +
                  16);
+}
+
+// The form d runs in: main_form, or FP64 log g in global memory when the
+// shared-memory lattice form's state does not fit.
+inline int fit_form(const MainDesc& d, int team)
+{
+  const int form = main_form(d);
+  return form == 0 && team_bytes(d, 0, team) > kSmemBytes ? 3 : form;
 }
 
 }  // namespace wlg

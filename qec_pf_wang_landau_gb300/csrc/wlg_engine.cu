@@ -319,7 +319,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   // resumable run: state saved at the end of a launch, restored at the start
   unsigned char* const st = d.off_state >= 0 ? statepool + d.off_state : nullptr;
   const StateLayout sl = state_layout(P, d.I, d.nwL, d.L);
-  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg, kTable ? d.N : 0, !kGlobalG);
+  const TeamLayout lay = team_layout(P, d.L, d.nwL, d.nwM, d.I, kReg ? 2 : d.nwL, kTable ? d.N : 0, !kGlobalG);
   // FP64 log g: in the team's shared memory, or (large problems) in this
   // resident team's slice of a global pool, L2-resident and touched only on
   // bin changes, averaging and exchange

@@ -122,7 +122,10 @@ WLG_HD inline int align16(int x) { return (x + 15) & ~15; }
 // reg_lattice: spins in a register (N <= 64); nbt_sites: sites of the
 // neighbour table (0 when the table is not used); g_in_smem: FP64 log g in
 // shared memory (else in a global pool).
-WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, bool reg_lattice, int nbt_sites,
+// lat_words: 32-bit words per walker of the lattice area (the lattice
+// itself, or the exchange staging of a register lattice); nbt_entries:
+// 16-byte neighbour-table entries.
+WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, int lat_words, int nbt_entries,
                                      bool g_in_smem = true)
 {
   TeamLayout t{};
@@ -134,7 +137,7 @@ WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, b
   t.off_H = o;
   o = align16(o + 4 * L * team);
   t.off_lat = o;
-  o = align16(o + 4 * (reg_lattice ? 2 : nwL) * team);
+  o = align16(o + 4 * lat_words * team);
   t.off_E = o;
   o = align16(o + 4 * team);
   t.off_perm = o;
@@ -144,7 +147,7 @@ WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, b
   t.off_J = o;
   o = align16(o + 4 * 2 * nwL);
   t.off_nbt = o;
-  o = align16(o + 16 * nbt_sites);
+  o = align16(o + 16 * nbt_entries);
   t.off_f = o;  // f [I], then ln f [I]
   o = align16(o + 16 * I);
   t.off_cond = o;

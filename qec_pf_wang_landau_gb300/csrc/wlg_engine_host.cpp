@@ -248,6 +248,23 @@ struct wlg_context {
   size_t used = 0;
   DevBuf buf[kSlots];
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {};          // main-run groups side by side
+  cudaEvent_t aux_ev[kAux + 1] = {};    // fork, then one join per aux stream
+  void release_aux()
+  {
+    for (auto& a : aux) {
+      if (a != nullptr) {
+        cudaStreamSynchronize(a);
+        cudaStreamDestroy(a);
+      }
+      a = nullptr;
+    }
+    for (auto& e : aux_ev) {
+      if (e != nullptr) cudaEventDestroy(e);
+      e = nullptr;
+    }
+  }
   float t_pre = 0, t_main = 0;
   double t_handoff = 0, t_stitch = 0;
   long long h2d = 0, d2h = 0;
@@ -301,6 +318,11 @@ struct ContextExec final : Exec {
     ev = c->ev;
     per_cta = &c->tuned;
     pool = &c->workers();
+    if (c->aux[0] != nullptr) {
+      aux = c->aux;
+      aux_ev = c->aux_ev;
+      n_aux = wlg_context::kAux;
+    }
   }
   wlg_status buffer(Slot slot, size_t bytes, void** out) override
   {
@@ -707,36 +729,22 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
   if (m == 0) return WLG_OK;
   int sms = 1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ex.device);
-  // variant: 0 spins in shared memory, 1 spins in a register, 2 register
-  // spins + neighbour table (4 distinct neighbours: X, Y >= 3)
-  auto variant_of = [](const MainDesc& d) { return d.N > 64 ? 0 : (d.X >= 3 && d.Y >= 3 ? 2 : 1); };
+  // one launch per (form, team size); the form by lattice storage (fit_form)
   std::map<std::pair<int, int>, std::vector<int>> groups;
-  for (int i = 0; i < m; ++i) groups[{variant_of(prep.main[i]), prep.main[i].team}].push_back(i);
+  for (int i = 0; i < m; ++i) groups[{wlg::fit_form(prep.main[i], prep.main[i].team), prep.main[i].team}].push_back(i);
   std::vector<int> order;
   // variant, team, bytes, per_cta, first, count, L (max compact bins)
   std::vector<std::tuple<int, int, int, int, int, int, int>> launches;
   for (const auto& [key, idx] : groups) {
-    int variant = key.first;
+    const int variant = key.first;
     const int team = key.second;
-    auto group_bytes = [&](bool g_in_smem) {
-      int b = 0;
-      for (int i : idx) {
-        const MainDesc& d = prep.main[i];
-        b = std::max(b, wlg::team_layout(team, d.L, d.nwL, d.nwM, d.I, variant == 1 || variant == 2,
-                                         variant == 2 ? d.N : 0, g_in_smem)
-                            .bytes +
-                          16);
-      }
-      return wlg::align16(b);
-    };
-    int bytes = group_bytes(true);
+    int bytes = 0;
     int Lmax = 1;
-    for (int i : idx) Lmax = std::max(Lmax, prep.main[i].L);
-    if (bytes > 227 * 1024 && variant == 0) {
-      variant = 3;  // FP64 log g moves to a global pool
-      bytes = group_bytes(false);
+    for (int i : idx) {
+      bytes = std::max(bytes, wlg::team_bytes(prep.main[i], variant, team));
+      Lmax = std::max(Lmax, prep.main[i].L);
     }
-    if (bytes > 227 * 1024) return fail(ex, WLG_ERR_INVALID, "problem state exceeds shared memory");
+    if (bytes > wlg::kSmemBytes) return fail(ex, WLG_ERR_INVALID, "problem state exceeds shared memory");
     int per_cta = team <= 256 ? 256 / team : 1;
     per_cta = std::min(per_cta, (227 * 1024) / bytes);
     if (team > 32) per_cta = std::min(per_cta, 15);
@@ -800,20 +808,34 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
     return st;
   auto launch_all = [&]() -> wlg_status {
     cudaMemsetAsync(d_next, 0, launches.size() * sizeof(int), ex.stream);
-    for (size_t g = 0; g < launches.size(); ++g) {
+    // groups side by side: a persistent launch's CTAs exit as its queue
+    // drains, and the next group's CTAs take the freed SMs during its tail
+    const int n_fork = ex.n_aux > 0 && launches.size() > 1 ? std::min<int>(ex.n_aux, static_cast<int>(launches.size())) : 0;
+    if (n_fork > 0) {
+      cudaEventRecord(ex.aux_ev[0], ex.stream);
+      for (int a = 0; a < n_fork; ++a) cudaStreamWaitEvent(ex.aux[a], ex.aux_ev[0], 0);
+    }
+    wlg_status s2 = WLG_OK;
+    for (size_t g = 0; g < launches.size() && s2 == WLG_OK; ++g) {
       const auto [variant, team, bytes, per_cta, first, count, Lmax] = launches[g];
       const int grid = grids[g];
       double* gp = variant == 3 ? static_cast<double*>(d_gpool) + gpool_off[g] : nullptr;
-      const wlg_status s2 = wlg::launch_main_batch(
+      s2 = wlg::launch_main_batch(
         variant, static_cast<const MainDesc*>(d_md), static_cast<const int*>(d_order) + first, count, team, bytes,
         per_cta, grid, static_cast<int*>(d_next) + g, gp, static_cast<long long>(Lmax) * team,
         static_cast<const uint32_t*>(d_Jw), static_cast<const uint32_t*>(d_latw), static_cast<const int*>(d_win),
         static_cast<const uint32_t*>(d_mask), static_cast<double*>(d_out), static_cast<MainResult*>(d_res),
-        static_cast<unsigned char*>(d_state), ex.stream);
-      if (s2 != WLG_OK) return fail(ex, s2, "main-run launch failed");
-      ++ex.launches;
-      ex.main_forms |= 1 << variant;
+        static_cast<unsigned char*>(d_state), n_fork > 0 ? ex.aux[g % n_fork] : ex.stream);
+      if (s2 == WLG_OK) {
+        ++ex.launches;
+        ex.main_forms |= 1 << variant;
+      }
     }
+    for (int a = 0; a < n_fork; ++a) {  // join (also after a failed launch)
+      cudaEventRecord(ex.aux_ev[1 + a], ex.aux[a]);
+      cudaStreamWaitEvent(ex.stream, ex.aux_ev[1 + a], 0);
+    }
+    if (s2 != WLG_OK) return fail(ex, s2, "main-run launch failed");
     return WLG_OK;
   };
   if (ex.ev != nullptr) cudaEventRecord(ex.ev[2], ex.stream);
@@ -910,6 +932,10 @@ wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context**
     }
     ctx->stream = ctx->own_stream;
     for (auto& e : ctx->ev) cudaEventCreate(&e);
+    bool aux_ok = true;
+    for (auto& a : ctx->aux) aux_ok = aux_ok && cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto& e : ctx->aux_ev) aux_ok = aux_ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!aux_ok) ctx->release_aux();  // launches then run one after another on the context's stream
     *out = ctx;
     return WLG_OK;
   });
@@ -923,6 +949,7 @@ wlg_status wlg_context_destroy(wlg_context* ctx)
   for (DevBuf& b : ctx->buf)
     if (b.p != nullptr) cudaFree(b.p);
   for (auto& e : ctx->ev) cudaEventDestroy(e);
+  ctx->release_aux();
   cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return WLG_OK;
@@ -1172,9 +1199,7 @@ wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, i
     std::map<std::pair<int, int>, std::vector<int>> groups;
     for (size_t i = 0; i < prep.main.size(); ++i) {
       const MainDesc& d = prep.main[i];
-      int form = main_form(d);
-      if (form == 0 && team_bytes(d, 0, d.team) > 227 * 1024) form = 3;
-      groups[{form == 3 ? 0 : form, d.team}].push_back(static_cast<int>(i));
+      groups[{fit_form(d, d.team), d.team}].push_back(static_cast<int>(i));
     }
     std::map<std::pair<int, int>, int> best;
     std::vector<wlg_tuning> found;
@@ -1188,10 +1213,7 @@ wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, i
       wlg_tuning t{key.first, key.second, 1, 0.0f, 0};
       float best_ms = 0.0f;
       for (int c = 1; c <= limit; c *= 2) {
-        std::map<std::pair<int, int>, int> force{{key, c}};
-        // the form recorded for the launch may be 3 when the team's state does
-        // not fit shared memory; force both keys
-        force[{3, key.second}] = c;
+        const std::map<std::pair<int, int>, int> force{{key, c}};
         ex.per_cta = &force;
         std::vector<MainResult> mres;
         std::vector<double> out_host;
@@ -1210,7 +1232,6 @@ wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, i
       }
       t.main_ms = best_ms;
       best[key] = t.per_cta;
-      best[{3, key.second}] = t.per_cta;
       found.push_back(t);
     }
     for (const auto& [k, v] : best) ctx->tuned[k] = v;

@@ -590,8 +590,7 @@ void wlg_server::finish_admission(AdmitJob& aj)
     }
     MainDesc d = prep.main[main_of[k]];
     const BlockLayout bl = block_layout(d.team, d.I, d.L, d.nwL, d.nwM);
-    int form = main_form(d);
-    if (team_bytes(d, form, d.team) > kSmemLimit && form == 0) form = 3;
+    const int form = fit_form(d, d.team);
     if (team_bytes(d, form, d.team) > kSmemLimit || bl.bytes > bb.bytes) {
       arena.release(boff, bb.bytes);
       class_done(id, cls, WLG_ERR_INVALID, 0, {});
