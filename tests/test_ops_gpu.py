@@ -442,3 +442,53 @@ def test_device_exp_of_nonnegative_is_at_least_one(cuda, probe):
     dl = torch.zeros_like(dx)
     assert probe.probe_exp_log(_dptr(dx), _dptr(de), _dptr(dl), len(x)) == 0
     assert (de.cpu().numpy() >= 1.0).all()
+
+
+@pytest.mark.parametrize("case", ["none", "all", "some"])
+def test_reset_cond_reference_cases(cuda, case):
+    """test_reset_d_cond.cu:22/50/79: 2 samples x 10 windows x 20 walkers,
+    beta 1e-10; factors at exp(beta) keep every flag, factors 1e-3 above it
+    reset every flag, and raising only the last sample's factors resets only
+    its windows."""
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    beta, R, I, W = 1e-10, 2, 10, 20
+    factor = np.full(R * I * W, np.exp(beta))
+    if case == "all":
+        factor += 1e-3
+    if case == "some":
+        factor[(R - 1) * I * W:] += 1e-3
+    cond = torch.ones(R * I, dtype=torch.int8, device="cuda")
+    f = torch.from_numpy(factor).cuda()
+    wlg.call("wlg_reset_cond", _dptr(cond), _dptr(f), R * I, C.c_double(beta), W, None)
+    torch.cuda.synchronize()
+    got = cond.cpu().numpy()
+    want = np.ones(R * I, np.int8)
+    if case == "all":
+        want[:] = 0
+    if case == "some":
+        want[(R - 1) * I:] = 0
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("case", ["all_finished", "last_not_finished", "none_finished"])
+def test_check_finished_reference_cases(cuda, case):
+    """test_check_interactions.cu:17/58/105: 100 samples x 20 windows; -1
+    marks a sample whose windows are all flat."""
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    R, I = 100, 20
+    cond = np.ones(R * I, np.int8) if case != "none_finished" else np.zeros(R * I, np.int8)
+    if case == "last_not_finished":
+        cond[-1] = 0
+    d_cond = torch.from_numpy(cond).cuda()
+    out = torch.zeros(R, dtype=torch.int32, device="cuda")
+    wlg.call("wlg_check_finished", _dptr(out), _dptr(d_cond), I, R, None)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    if case == "all_finished":
+        assert (got == -1).all()
+    elif case == "last_not_finished":
+        assert (got[:-1] == -1).all() and got[-1] == I - 1
+    else:
+        assert (got == 0).all()
