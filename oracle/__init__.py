@@ -3,7 +3,7 @@
 ctypes binding to ``liboracle.so``, the CPU restatement of the reference's
 replica-exchange Wang-Landau path (oracle.cpp, oracle_host.cpp).  Only the
 test-suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
-it, as the checker; the engine never imports it.
+it, to compare the engine's results with; the engine never imports it.
 
 ``build()`` is the build recipe: one g++ invocation, no external libraries.
 Host float arithmetic is compiled with ``-ffp-contract=off`` so that the

@@ -3,7 +3,8 @@
 // A plain C++ restatement of the reference's replica-exchange Wang-Landau path
 // (dfki-ric-quantum/qec_pf_wang_landau, src/wl.cu, src/interval.cpp,
 // src/file_io.cpp, src/result_handling.cpp), used by tests/, by
-// __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+// __graft_entry__.smoke() and by bench.py's CPU-baseline leg, to compare the
+// engine's results with.
 // It is never linked into, loaded by or called from the product library.
 //
 // Every function works on the reference's own data layout (int8 spins and

@@ -4,8 +4,8 @@
 // /Histogram/<k>, /Interaction/<k>, /Lattice/<k>/<E>, each holding one 1-D
 // dataset) and mainrun_results.h5 (utils.cpp:137-236: /<k>/<seed>/<time>/log_g,
 // a 1-D dataset of compound {Key: int32, Value: float64} with a 256-byte
-// string attribute CodeVersion).  Neither machine of this build has libhdf5,
-// so this module writes and reads exactly those shapes itself, following the
+// string attribute CodeVersion).  It does not depend on libhdf5: this module
+// writes and reads exactly those shapes itself, following the
 // public HDF5 File Format Specification (version 3.0): a version-2
 // superblock, version-2 object headers, groups with compact link storage
 // (Link Info, Group Info and Link messages), contiguous dataset storage, and

@@ -1,6 +1,6 @@
 """HDF5 result files without libhdf5 (qec_pf_wang_landau_gb300/csrc/wlg_h5.*).
 
-Neither machine of this build has libhdf5 or h5py, so the writer follows the
+No libhdf5 or h5py is available to these tests, so the writer follows the
 public HDF5 File Format Specification and is checked three ways: its
 checksum against lookup3's published test vectors, a round trip through the
 engine's own reader, and an independent parse of the superblock, object
