@@ -223,6 +223,43 @@ def test_engine_random_configs_bit_exact_in_one_batch(cuda):
     assert compared >= 8
 
 
+EDGE = [
+    # two rows: the up and down neighbours of a site coincide (periodic), or one is missing (open)
+    (2, 5, 0, 0.1, "i", 11, 2, 32, 8, 2000, 3, 3, 0.25, 0.8, 1e-3, 500, 1, 1, 0),
+    (2, 2, 1, 0.2, "h", 12, 2, 32, 4, 1000, 2, 2, 0.5, 0.8, 1e-3, 300, 1, 1, 0),
+    (5, 2, 1, 0.1, "c", 13, 1, 32, 8, 2000, 3, 2, 0.25, 0.8, 1e-3, 300, 2, 1, 0),
+    # the largest lattice (4096 spins; 16 pre-run walkers fit one SM's shared memory)
+    (64, 64, 0, 0.05, "i", 21, 1, 16, 16, 2000, 4, 8, 0.25, 0.8, 1e-3, 100, 1, 1, 0),
+]
+
+
+@pytest.mark.parametrize("cfg", EDGE, ids=[f"{c[0]}x{c[1]}b{c[2]}" for c in EDGE])
+def test_edge_lattices_bit_exact(cuda, cfg):
+    """Two-row lattices and the maximum size against the oracle's run, capped
+    at 2 outer iterations: per-window log g and move counts bit for bit."""
+    import qec_pf_wang_landau_gb300 as wlg
+    I, W = cfg[10], cfg[11]
+    ref = oracle_run(*cfg, max_outer=2)
+    assert ref["status"] == 3, ref["status"]  # ran until the cap
+    out = wlg.Context(0).solve_raw(big_problems(cfg, max_outer=2))
+    assert sum(r.flips for r, _, _, _ in out) == ref["flips"]
+    for k, (res, s, e, wins) in enumerate(out):
+        assert res.status == wlg.WLG_ERR_TIMEOUT
+        assert np.array_equal(s, ref["start"][k * I:(k + 1) * I]) and np.array_equal(e, ref["end"][k * I:(k + 1) * I])
+        for b in range(I):
+            o = ref["off_hist"][(k * I + b) * W]
+            assert np.array_equal(wins[b], ref["logG"][o:o + (e[b] - s[b] + 1)]), (k, b)
+
+
+def test_empty_batch(cuda):
+    import qec_pf_wang_landau_gb300 as wlg
+    ctx = wlg.Context(0)
+    assert ctx.solve([]) == []
+    assert ctx.solve_raw([]) == []
+    with wlg.Server(0) as srv:
+        assert srv.submit([]) == []
+
+
 def test_engine_heterogeneous_batch_equals_separate_runs(cuda):
     """Problems of different shapes in one batch give the same results as alone."""
     import qec_pf_wang_landau_gb300 as wlg
