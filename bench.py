@@ -527,20 +527,33 @@ def run_reference(args):
 def profile_case(name: str):
     """Small fixed cases for ncu captures (not bench numbers): `main6x6` = 152
     problems of the workload (samples 0-37 x ivhc, one per SM) capped at 20
-    outer iterations, solved twice (capture the second main-run launch)."""
+    outer iterations; `large16` = the large-lattice leg's 152 16x16 problems
+    (512-thread teams) capped at 3 outer iterations.  Each is solved twice
+    (capture the second main-run launch)."""
     import qec_pf_wang_landau_gb300 as wlg
     wlg.build()
-    if name != "main6x6":
+    if name == "main6x6":
+        probs = problems(0)[:152]
+        cap = 20
+    elif name == "large16":
+        c = LARGE
+        probs = [wlg.problem(16, 16, prob=c["prob"], error_class=cl, seed=c["seed"], sample=k, pre_walkers=128,
+                             pre_intervals=128, pre_iterations=100 * 256, intervals=64, walkers_per_interval=8,
+                             overlap=0.3, alpha=0.8, beta=1e-8, iterations=1000, exchange_every=10)
+                 for k in range(c["samples"]) for cl in "ivhc"]
+        cap = 3
+    else:
         raise SystemExit(f"unknown profile case {name}")
-    probs = problems(0)[:152]
     for p in probs:
-        p.max_outer = 20
+        p.max_outer = cap
     ctx = wlg.Context(0)
     for _ in range(2):
         out = ctx.solve_raw(probs)
     st = ctx.stats()
-    steps = sum(r.flips for r, _, _, _ in out) / 30
-    print(json.dumps({"case": name, "main_ms": st["main_ms"], "walker_steps_per_warp": steps / len(probs)}))
+    walkers = probs[0].intervals * probs[0].walkers_per_interval
+    steps = sum(r.flips for r, _, _, _ in out) / walkers
+    print(json.dumps({"case": name, "main_ms": st["main_ms"], "main_forms": st["main_forms"],
+                      "walker_steps_per_problem": steps / len(probs)}))
 
 
 def main():
