@@ -194,3 +194,32 @@ def test_served_stitching_modes_equal_batch_engine(cuda):
             assert np.array_equal(np.array(d.log_probs), lp)
     with pytest.raises(wlg.WlgError):
         wlg.Server(0, stitching=7)
+
+
+def test_concurrent_submitters_get_the_sequential_results(cuda):
+    """Four host threads submit and poll at once (ctypes releases the GIL in
+    the calls): every request retires once, with the bits it gets alone."""
+    import threading
+    import qec_pf_wang_landau_gb300 as wlg
+    reqs = [request(wlg, 4 + (k % 3), 4 + (k % 2), k, boundary=k % 2, intervals=4) for k in range(12)]
+    with wlg.Server(0) as srv:
+        ids = srv.submit(reqs)
+        alone = srv.wait(ids, 300)
+    got, errors = {}, []
+    with wlg.Server(0) as srv:
+        def worker(part):
+            try:
+                mine = srv.submit([reqs[k] for k in part])
+                got.update({k: rid for k, rid in zip(part, mine)})
+            except Exception as e:  # noqa: BLE001 - reported below
+                errors.append(e)
+        threads = [threading.Thread(target=worker, args=(list(range(w, 12, 4)),)) for w in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        assert not errors, errors
+        done = srv.wait(list(got.values()), 300)
+        assert srv.stats()["completed"] == 12
+    for k, rid in got.items():
+        assert same(as_tuple(done[rid]), as_tuple(alone[ids[k]])), k
