@@ -337,6 +337,12 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   double* lnfw = fwin + d.I;  // log(f) of each window, recomputed only when f changes
   int* cond = reinterpret_cast<int*>(base + lay.off_cond);
   int* flat = reinterpret_cast<int*>(base + lay.off_flat);
+  // A finished window (cond stays 1) is frozen: its walkers no longer change
+  // log g, so once an averaging pass leaves every value as it was, every
+  // later pass would too; such windows are skipped (stab).  Not saved with a
+  // suspended run: a resumed one recomputes one pass, with the same result.
+  int* stab = reinterpret_cast<int*>(base + lay.off_stab);
+  int* chg = stab + d.I;
   int* win = reinterpret_cast<int*>(base + lay.off_win);  // start, end, base, Lb, E0
   int* misc = reinterpret_cast<int*>(base + lay.off_misc);
   const int I = d.I, W = d.W;
@@ -354,6 +360,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     lnfw[q] = log(kE);
     cond[q] = 0;
     flat[q] = 0;
+    stab[q] = 0;
+    chg[q] = 0;
   }
   const bool resumed = st != nullptr && reinterpret_cast<const int*>(st)[4] != 0;
   for (int c = 0; c < d.L; ++c) {
@@ -665,17 +673,24 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     for (int q = t; q < I * d.L; q += P) {
       const int wb = q / d.L;
       const int c = q - wb * d.L;
-      if (cond[wb] != 1 || c >= w_len[wb]) continue;
+      if (cond[wb] != 1 || stab[wb] != 0 || c >= w_len[wb]) continue;
       double avg = 0.0;
       if (mask_has(mask, ((w_base[wb] - d.e_min) >> d.lg) + c)) {
         for (int v = 0; v < W; ++v) avg += G[c * P + wb * W + v] / W;
       }
-      for (int v = 0; v < W; ++v) G[c * P + wb * W + v] = avg;
+      bool same = true;
+      for (int v = 0; v < W; ++v) {
+        same = same && __double_as_longlong(G[c * P + wb * W + v]) == __double_as_longlong(avg);
+        G[c * P + wb * W + v] = avg;
+      }
+      if (!same) chg[wb] = 1;
     }
     team.sync();
     // ---- reset and convergence (wl.cu:596-613, :662-708, mainrun.cu:243, :342-344)
     if (t < I) {
       if (cond[t] == 1 && fwin[t] > reset_lim) cond[t] = 0;
+      stab[t] = cond[t] == 1 && (stab[t] != 0 || chg[t] == 0) ? 1 : 0;
+      chg[t] = 0;
       flat[t] = 0;
     }
     team.sync();

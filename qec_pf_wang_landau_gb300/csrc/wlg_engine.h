@@ -112,8 +112,8 @@ WLG_HD inline StateLayout state_layout(int P, int I, int nwL, int L)
 
 // Team shared-memory layout of a problem (bytes, 16-byte aligned pieces).
 struct TeamLayout {
-  int off_G, off_Gf, off_H, off_lat, off_E, off_perm, off_mask, off_J, off_nbt, off_f, off_cond, off_flat, off_win,
-    off_misc;
+  int off_G, off_Gf, off_H, off_lat, off_E, off_perm, off_mask, off_J, off_nbt, off_f, off_cond, off_flat, off_stab,
+    off_win, off_misc;
   int bytes;
 };
 
@@ -154,6 +154,8 @@ WLG_HD inline TeamLayout team_layout(int team, int L, int nwL, int nwM, int I, i
   o = align16(o + 4 * I);
   t.off_flat = o;
   o = align16(o + 4 * I);
+  t.off_stab = o;  // per window: averaging is a fixed point [I], then changed-in-this-pass [I]
+  o = align16(o + 8 * I);
   t.off_win = o;
   o = align16(o + 4 * 5 * I);
   t.off_misc = o;
