@@ -109,3 +109,45 @@ def test_mainrun_time_limit_and_flags(cuda, tmp_path):
     assert run("wlg_mainrun", ["-x", "4"], tmp_path).returncode == 0
     # no pre-run file for another seed: failure
     assert run("wlg_mainrun", [a if a != str(SEED) else "999" for a in MAIN], tmp_path).returncode != 0
+
+
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_decode_program_equals_served_requests(cuda, tmp_path, boundary):
+    """bin/wlg_decode: syndromes read from a file (comments and blank lines
+    skipped), patterns built from them, served, one line per syndrome in
+    input order: the same class log-probabilities as the same requests sent
+    through the server's Python binding, and the most likely class."""
+    import qec_pf_wang_landau_gb300 as wlg
+    Xd, Yd, p = 5, 5, 0.08
+    syn = []
+    for k in range(5):
+        Jk = O.init_interactions(Xd, Yd, k + 1, 777, p, "i")[k * 2 * Xd * Yd:(k + 1) * 2 * Xd * Yd]
+        syn.append(wlg.frustration(Xd, Yd, boundary, Jk))
+    f = tmp_path / "syndromes.txt"
+    f.write_text("# five syndromes\n\n" + "\n".join("".join(str(int(b)) for b in s) for s in syn) + "\n")
+    out = run("wlg_decode", ["-x", str(Xd), "-y", str(Yd), "-p", str(p), "--boundary", str(boundary), "-f", str(f),
+                             "-b", "0.001", "-s", "3"], str(tmp_path))
+    assert out.returncode == 0, out.stderr
+    lines = [ln.split() for ln in out.stdout.strip().splitlines()]
+    assert [int(ln[0]) for ln in lines] == list(range(5))
+    reqs = [wlg.problem(Xd, Yd, boundary=boundary, prob=p, seed=3, sample=k, pre_walkers=128, pre_intervals=32,
+                        pre_iterations=100 * Xd * Yd, intervals=4, walkers_per_interval=4, overlap=0.25, alpha=0.8,
+                        beta=1e-3, iterations=1000, exchange_every=10, exchange_mode=1, global_parity=0)
+            for k in range(5)]
+    pats = [wlg.couplings_from_syndrome(Xd, Yd, boundary, s) for s in syn]
+    with wlg.Server(0) as srv:
+        ids = srv.submit(reqs, couplings=pats)
+        got = srv.wait(ids, 300)
+    for ln, i in zip(lines, ids):
+        d = got[i]
+        assert int(ln[1]) == d.status
+        if d.status != 0:
+            continue
+        lp = [float(x) for x in ln[2:6]]
+        assert np.allclose(lp, list(d.log_probs), rtol=1e-9, atol=1e-12)
+        assert ln[6] == "ivhc"[int(np.argmax(d.log_probs))]
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1" + "0" * (Xd * Yd - 1) + "\n")  # one defect
+    out = run("wlg_decode", ["-x", str(Xd), "-y", str(Yd), "-p", str(p), "-f", str(bad)], str(tmp_path))
+    if boundary == 0:
+        assert out.returncode != 0 and "even" in out.stderr
