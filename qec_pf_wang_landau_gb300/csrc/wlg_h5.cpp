@@ -608,7 +608,10 @@ std::string read_file(const std::string& path, Group& root)
   while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) file.insert(file.end(), buf, buf + n);
   std::fclose(f);
   if (file.size() < kSuperblock || std::memcmp(file.data(), kSignature, 8) != 0) return "not an HDF5 file";
-  if (file[8] != 2 && file[8] != 3) return "superblock version (only 2 and 3 are read)";
+  if (file[8] != 2 && file[8] != 3)
+    return "superblock version " + std::to_string(file[8]) +
+           " (only 2 and 3 are read; files from libhdf5's default settings use 0: write the pre-run file with "
+           "wlg_prerun)";
   if (file[9] != 8 || file[10] != 8) return "offset/length sizes";
   In in{file, 12};
   in.le(8);
