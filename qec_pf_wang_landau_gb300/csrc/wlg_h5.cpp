@@ -470,39 +470,160 @@ bool parse_type(In& in, Type& t)
   return false;
 }
 
+// A header message: type and the byte range of its body.
+struct HMsg {
+  unsigned type;
+  uint64_t body, size;
+};
+
+constexpr unsigned kContinuation = 0x10;
+constexpr unsigned kSymbolTable = 0x11;
+
+uint32_t le32_at(const std::vector<uint8_t>& f, uint64_t a)
+{
+  return static_cast<uint32_t>(f[a]) | static_cast<uint32_t>(f[a + 1]) << 8 | static_cast<uint32_t>(f[a + 2]) << 16 |
+         static_cast<uint32_t>(f[a + 3]) << 24;
+}
+
+// The messages of the object header at addr, version 2 ("OHDR", IV.A.1.b,
+// continuation blocks "OCHK") or version 1 (IV.A.1.a: no signature, 8-byte
+// aligned messages, continuation blocks of bare messages), in order.
+std::string header_messages(const std::vector<uint8_t>& file, uint64_t addr, std::vector<HMsg>& out)
+{
+  out.clear();
+  if (addr + 16 > file.size()) return "object header address";
+  std::vector<std::pair<uint64_t, uint64_t>> blocks;  // message ranges still to read
+  const bool v2 = std::memcmp(file.data() + addr, "OHDR", 4) == 0;
+  unsigned crt = 0;
+  if (v2) {
+    In in{file, addr + 4};
+    const unsigned version = static_cast<unsigned>(in.le(1));
+    const unsigned flags = static_cast<unsigned>(in.le(1));
+    if (version != 2) return "object header version";
+    if (flags & 0x20) in.le(16);
+    if (flags & 0x10) in.le(4);
+    const uint64_t chunk = in.le(1 << (flags & 3));
+    crt = (flags & 0x04) ? 2 : 0;
+    const uint64_t msg_start = in.pos, msg_end = in.pos + chunk;
+    if (!in.ok || msg_end + 4 > file.size()) return "object header size";
+    if (lookup3(file.data() + addr, msg_end - addr) != le32_at(file, msg_end)) return "object header checksum";
+    blocks.emplace_back(msg_start, msg_end);
+  } else {
+    In in{file, addr};
+    if (in.le(1) != 1) return "object header version";
+    in.le(1);
+    in.le(2);  // message count (the blocks' sizes bound the reading)
+    in.le(4);  // reference count
+    const uint64_t size = in.le(4);
+    if (!in.ok || addr + 16 + size > file.size()) return "object header size";
+    blocks.emplace_back(addr + 16, addr + 16 + size);
+  }
+  for (size_t bi = 0; bi < blocks.size(); ++bi) {
+    if (bi > 64) return "too many continuation blocks";
+    auto [pos, end] = blocks[bi];
+    if (v2 && bi > 0) {  // "OCHK", messages, checksum
+      if (end < pos + 8 || std::memcmp(file.data() + pos, "OCHK", 4) != 0) return "continuation block";
+      if (lookup3(file.data() + pos, end - 4 - pos) != le32_at(file, end - 4)) return "continuation checksum";
+      pos += 4;
+      end -= 4;
+    }
+    In in{file, pos};
+    const uint64_t head = v2 ? 4 + crt : 8;
+    while (in.pos + head <= end) {
+      unsigned type;
+      uint64_t size;
+      if (v2) {
+        type = static_cast<unsigned>(in.le(1));
+        size = in.le(2);
+        in.le(1);
+        in.le(static_cast<int>(crt));
+      } else {
+        type = static_cast<unsigned>(in.le(2));
+        size = in.le(2);
+        in.le(1);
+        in.le(3);
+      }
+      const uint64_t body = in.pos;
+      if (!in.ok || body + size > end) return "message size";
+      if (type == kContinuation) {
+        In c{file, body};
+        const uint64_t at = c.le(8), len = c.le(8);
+        if (!c.ok || at + len > file.size()) return "continuation address";
+        blocks.emplace_back(at, at + len);
+      } else if (type != kNil) {
+        out.push_back({type, body, size});
+      }
+      in.pos = body + size;
+    }
+  }
+  return "";
+}
+
+// Links of an old-style group (III.A.1 version-1 B-tree of group nodes,
+// III.B symbol table nodes, III.D local heap for the names).
+std::string symbol_table_links(const std::vector<uint8_t>& file, uint64_t btree, uint64_t heap,
+                               std::vector<std::pair<std::string, uint64_t>>& links, int depth)
+{
+  if (depth > 32) return "B-tree too deep";
+  if (heap + 32 > file.size() || std::memcmp(file.data() + heap, "HEAP", 4) != 0) return "local heap";
+  In h{file, heap + 8};
+  const uint64_t seg_size = h.le(8);
+  h.le(8);
+  const uint64_t seg = h.le(8);
+  if (!h.ok || seg + seg_size > file.size()) return "local heap segment";
+  if (btree + 24 > file.size() || std::memcmp(file.data() + btree, "TREE", 4) != 0) return "group B-tree";
+  In t{file, btree + 4};
+  const unsigned type = static_cast<unsigned>(t.le(1));
+  const unsigned level = static_cast<unsigned>(t.le(1));
+  const uint64_t used = t.le(2);
+  t.le(8);
+  t.le(8);
+  if (type != 0) return "B-tree node type";
+  for (uint64_t k = 0; k < used; ++k) {
+    t.le(8);  // key: heap offset of the largest name in the child
+    const uint64_t child = t.le(8);
+    if (!t.ok) return "B-tree node";
+    if (level > 0) {
+      const std::string err = symbol_table_links(file, child, heap, links, depth + 1);
+      if (!err.empty()) return err;
+      continue;
+    }
+    if (child + 8 > file.size() || std::memcmp(file.data() + child, "SNOD", 4) != 0) return "symbol table node";
+    In sn{file, child + 4};
+    if (sn.le(1) != 1) return "symbol table node version";
+    sn.le(1);
+    const uint64_t nsym = sn.le(2);
+    for (uint64_t e = 0; e < nsym; ++e) {
+      const uint64_t name_off = sn.le(8);
+      const uint64_t obj = sn.le(8);
+      sn.le(4);
+      sn.le(4);
+      sn.le(16);
+      if (!sn.ok || name_off >= seg_size) return "symbol table entry";
+      const char* nm = reinterpret_cast<const char*>(file.data() + seg + name_off);
+      links.emplace_back(std::string(nm, strnlen(nm, seg_size - name_off)), obj);
+    }
+  }
+  return "";
+}
+
 std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group* g, Dataset* d, int depth,
                          bool* is_group)
 {
   if (depth > 64) return "nesting too deep";
-  if (addr + 10 > file.size() || std::memcmp(file.data() + addr, "OHDR", 4) != 0) return "no object header";
-  In in{file, addr + 4};
-  const unsigned version = static_cast<unsigned>(in.le(1));
-  const unsigned flags = static_cast<unsigned>(in.le(1));
-  if (version != 2) return "object header version";
-  if (flags & 0x20) in.le(16);
-  if (flags & 0x10) in.le(4);
-  const uint64_t chunk = in.le(1 << (flags & 3));
-  const uint64_t msg_start = in.pos, msg_end = in.pos + chunk;
-  if (!in.ok || msg_end + 4 > file.size()) return "object header size";
-  const uint32_t sum = static_cast<uint32_t>(file[msg_end]) | static_cast<uint32_t>(file[msg_end + 1]) << 8 |
-                       static_cast<uint32_t>(file[msg_end + 2]) << 16 | static_cast<uint32_t>(file[msg_end + 3]) << 24;
-  if (lookup3(file.data() + addr, msg_end - addr) != sum) return "object header checksum";
+  std::vector<HMsg> msgs;
+  std::string herr = header_messages(file, addr, msgs);
+  if (!herr.empty()) return herr;
   std::vector<std::pair<std::string, uint64_t>> links;
   bool has_layout = false;
   Type type = Type::u8;
   uint64_t count = 0, data_addr = kUndef, data_size = 0;
+  std::vector<uint8_t> compact;
+  bool is_compact = false;
   std::map<std::string, std::string> attrs;
-  in.pos = msg_start;
-  const unsigned crt = (flags & 0x04) ? 2 : 0;
-  while (in.pos + 4 + crt <= msg_end) {
-    const unsigned mtype = static_cast<unsigned>(in.le(1));
-    const uint64_t size = in.le(2);
-    in.le(1);
-    in.le(static_cast<int>(crt));
-    const uint64_t body = in.pos;
-    if (body + size > msg_end) return "message size";
-    In m{file, body};
-    switch (mtype) {
+  for (const HMsg& msg : msgs) {
+    In m{file, msg.body};
+    switch (msg.type) {
       case kLink: {
         const unsigned lv = static_cast<unsigned>(m.le(1));
         const unsigned lf = static_cast<unsigned>(m.le(1));
@@ -519,15 +640,26 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
         links.emplace_back(name, m.le(8));
         break;
       }
+      case kSymbolTable: {
+        const uint64_t bt = m.le(8), hp = m.le(8);
+        if (!m.ok) break;
+        const std::string err = symbol_table_links(file, bt, hp, links, 0);
+        if (!err.empty()) return err;
+        break;
+      }
       case kDataspace: {
         const unsigned sv = static_cast<unsigned>(m.le(1));
         const unsigned rank = static_cast<unsigned>(m.le(1));
-        m.le(1);
-        if (sv != 2) return "dataspace version";
-        m.le(1);
+        m.le(1);  // flags
+        if (sv == 1) {
+          m.le(5);  // reserved
+        } else if (sv == 2) {
+          m.le(1);  // type
+        } else {
+          return "dataspace version";
+        }
         count = 1;
         for (unsigned r = 0; r < rank; ++r) count *= m.le(8);
-        if (rank == 0) count = 1;
         break;
       }
       case kDatatype:
@@ -536,9 +668,16 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
       case kLayout: {
         const unsigned lv = static_cast<unsigned>(m.le(1));
         const unsigned cls = static_cast<unsigned>(m.le(1));
-        if (lv != 3 || cls != 1) return "unsupported layout";
-        data_addr = m.le(8);
-        data_size = m.le(8);
+        if (lv != 3 || cls > 1) return "unsupported layout";
+        if (cls == 1) {
+          data_addr = m.le(8);
+          data_size = m.le(8);
+        } else {  // compact: the data is in the message
+          data_size = m.le(2);
+          if (!m.need(data_size)) return "compact data";
+          compact.assign(file.begin() + static_cast<long>(m.pos), file.begin() + static_cast<long>(m.pos + data_size));
+          is_compact = true;
+        }
         has_layout = true;
         break;
       }
@@ -546,13 +685,15 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
         const unsigned av = static_cast<unsigned>(m.le(1));
         m.le(1);
         const uint64_t nsz = m.le(2), tsz = m.le(2), ssz = m.le(2);
-        if (av != 3) return "attribute version";
-        m.le(1);
-        if (!m.need(nsz + tsz + ssz)) return "attribute";
-        std::string name(reinterpret_cast<const char*>(file.data() + m.pos));
-        m.pos += nsz;
+        if (av < 1 || av > 3) return "attribute version";
+        if (av == 3) m.le(1);
+        auto pad = [av](uint64_t n) { return av == 1 ? (n + 7) / 8 * 8 : n; };
+        if (!m.need(pad(nsz) + pad(tsz) + pad(ssz))) return "attribute";
+        std::string name(reinterpret_cast<const char*>(file.data() + m.pos), strnlen(reinterpret_cast<const char*>(
+                                                                                   file.data() + m.pos), nsz));
+        m.pos += pad(nsz);
         const uint64_t dt = m.pos;
-        m.pos += tsz + ssz;
+        m.pos += pad(tsz) + pad(ssz);
         if ((file[dt] & 0x0f) == 3) {
           const uint64_t len = static_cast<uint64_t>(file[dt + 4]) | static_cast<uint64_t>(file[dt + 5]) << 8;
           if (m.need(len)) {
@@ -567,7 +708,6 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
         break;
     }
     if (!m.ok) return "truncated message";
-    in.pos = body + size;
   }
   *is_group = !has_layout;
   if (has_layout) {
@@ -576,7 +716,9 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
     d->count = count;
     d->string_attrs = attrs;
     if (data_size != count * elem_size(type)) return "dataset size";
-    if (data_size > 0) {
+    if (is_compact) {
+      d->bytes = compact;
+    } else if (data_size > 0) {
       if (data_addr == kUndef || data_addr + data_size > file.size()) return "dataset address";
       d->bytes.assign(file.begin() + static_cast<long>(data_addr), file.begin() + static_cast<long>(data_addr + data_size));
     }
@@ -608,18 +750,33 @@ std::string read_file(const std::string& path, Group& root)
   while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) file.insert(file.end(), buf, buf + n);
   std::fclose(f);
   if (file.size() < kSuperblock || std::memcmp(file.data(), kSignature, 8) != 0) return "not an HDF5 file";
-  if (file[8] != 2 && file[8] != 3)
-    return "superblock version " + std::to_string(file[8]) +
-           " (only 2 and 3 are read; files from libhdf5's default settings use 0: write the pre-run file with "
-           "wlg_prerun)";
-  if (file[9] != 8 || file[10] != 8) return "offset/length sizes";
-  In in{file, 12};
-  in.le(8);
-  in.le(8);
-  in.le(8);
-  const uint64_t root_addr = in.le(8);
-  const uint32_t sum = static_cast<uint32_t>(in.le(4));
-  if (lookup3(file.data(), 44) != sum) return "superblock checksum";
+  uint64_t root_addr = 0;
+  if (file[8] == 0 || file[8] == 1) {
+    // II.A.1 superblock version 0/1 (libhdf5's default): sizes at 13-14,
+    // base address at 24 (28 for version 1), then free space, end of file and
+    // driver addresses, then the root group's symbol table entry
+    if (file[13] != 8 || file[14] != 8) return "offset/length sizes";
+    const uint64_t base_at = file[8] == 0 ? 24 : 28;
+    if (file.size() < base_at + 32 + 40) return "superblock size";
+    In in{file, base_at};
+    if (in.le(8) != 0) return "base address";
+    in.le(8);
+    in.le(8);
+    in.le(8);
+    in.le(8);  // root entry: link name offset
+    root_addr = in.le(8);
+  } else if (file[8] == 2 || file[8] == 3) {
+    if (file[9] != 8 || file[10] != 8) return "offset/length sizes";
+    In in{file, 12};
+    in.le(8);
+    in.le(8);
+    in.le(8);
+    root_addr = in.le(8);
+    const uint32_t sum = static_cast<uint32_t>(in.le(4));
+    if (lookup3(file.data(), 44) != sum) return "superblock checksum";
+  } else {
+    return "superblock version " + std::to_string(file[8]);
+  }
   root.groups.clear();
   root.datasets.clear();
   bool is_group = false;

@@ -9,8 +9,12 @@
 // public HDF5 File Format Specification (version 3.0): a version-2
 // superblock, version-2 object headers, groups with compact link storage
 // (Link Info, Group Info and Link messages), contiguous dataset storage, and
-// Jenkins' lookup3 checksums.  The reader accepts the files this writer
-// produces (it is not a general HDF5 reader).
+// Jenkins' lookup3 checksums.  The reader accepts those files and the
+// structure libhdf5 writes by default for the same layouts (superblock 0,
+// version-1 object headers with continuation blocks, symbol-table groups
+// through version-1 B-trees and a local heap, version-1 dataspaces and
+// attributes, compact or contiguous storage); it is not a general HDF5
+// reader (no chunked storage, no dense link storage, no other types).
 #pragma once
 
 #include <cstdint>

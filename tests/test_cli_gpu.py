@@ -97,6 +97,41 @@ def test_mainrun_program_writes_the_engine_result(cuda, tmp_path, xmode):
         assert len(wlg.h5_list(path, f"{k}/{SEED}")[0]) == 2
 
 
+def test_mainrun_reads_a_prerun_file_in_libhdf5_default_structure(cuda, tmp_path):
+    """The pre-run file rewritten in the structure libhdf5 writes by default
+    (superblock 0, version-1 object headers, symbol-table groups; the
+    reference's own prerun output) gives the same main-run file."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import h5v0
+    import qec_pf_wang_landau_gb300 as wlg
+    assert run("wlg_prerun", PRE, tmp_path).returncode == 0
+    pre = str(tmp_path / "init" / SUB / "prerun_results.h5")
+
+    def tree(prefix):
+        groups, datasets = wlg.h5_list(pre, prefix)
+        out = {g: tree(f"{prefix}/{g}") for g in groups}
+        out.update({d: h5v0.Dataset(wlg.h5_read(pre, f"{prefix}/{d}")) for d in datasets})
+        return out
+
+    t = tree("")
+    os.remove(pre)
+    h5v0.write(pre, t)
+    with open(pre, "rb") as f:
+        assert f.read(9)[8] == 0  # superblock version 0
+    r = run("wlg_mainrun", MAIN + ["--exchange-mode", "0"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    path = str(tmp_path / "results" / SUB / "mainrun_results.h5")
+    ref = batch_solve(wlg, 0)
+    samples = sorted(int(g) for g in wlg.h5_list(path)[0])
+    assert samples == [k for k, (res, _, _) in enumerate(ref) if res.status == 0]
+    for k in samples:
+        (stamp,), _ = wlg.h5_list(path, f"{k}/{SEED}")
+        kv = wlg.h5_read(path, f"{k}/{SEED}/{stamp}/log_g")
+        _, E, G = ref[k]
+        assert np.array_equal(kv["Key"], E) and np.array_equal(kv["Value"], G)
+
+
 def test_mainrun_time_limit_and_flags(cuda, tmp_path):
     assert run("wlg_prerun", PRE, tmp_path).returncode == 0
     # -f 0: the run stops at the first check; no sample converges, nothing is written
