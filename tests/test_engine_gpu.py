@@ -396,3 +396,26 @@ def test_plain_form_equals_batched_form(cuda, cls, xc, xmode, gpar, I):
         assert r1.status == r2.status == 0
         assert r1.outer_iterations == r2.outer_iterations and r1.flips == r2.flips
         assert np.array_equal(E1, E2) and np.array_equal(G1, G2)
+
+
+def test_full_bench_workload_properties(cuda):
+    """The bench workload at its full size (6x6 periodic, p = 0.04, 100 samples
+    x 4 classes): every problem converges; every stitched log g has exactly the
+    energies the lattice can reach (exact transfer-matrix counts) and
+    logsumexp = N ln 2; each sample's four class probabilities sum to 1."""
+    import qec_pf_wang_landau_gb300 as wlg
+    probs = [wlg.problem(6, 6, prob=0.04, error_class=c, seed=12345, sample=k, pre_walkers=128, pre_intervals=32,
+                         pre_iterations=1000, intervals=10, walkers_per_interval=3, overlap=0.25, alpha=0.8,
+                         beta=1e-3, iterations=1000, exchange_every=20, exchange_mode=1)
+             for k in range(100) for c in "ivhc"]
+    out = wlg.Context(0).solve(probs)
+    assert all(r.status == 0 for r, _, _ in out)
+    J = {c: O.init_interactions(6, 6, 100, 12345, 0.04, c) for c in "ivhc"}
+    for q, (r, E, G) in enumerate(out):
+        k, c = divmod(q, 4)
+        cnt = O.exact_counts(J["ivhc"[c]][k * 72:(k + 1) * 72], 6, 6, 0)
+        assert set(E.tolist()) == set((np.nonzero(cnt)[0] - 72).tolist()), q
+        assert abs(np.logaddexp.reduce(G) - 36 * np.log(2)) < 1e-9
+    for k in range(100):
+        _, lp = wlg.class_log_probs([(E, G) for _, E, G in out[4 * k:4 * k + 4]], 0.04)
+        assert abs(np.logaddexp.reduce(lp)) < 1e-12
