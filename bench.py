@@ -427,13 +427,18 @@ def run_ours(args):
     if dist is not None:
         (t_dev, t_e2e, t_main), (converged, flips) = reduce_over_ranks(dist, [t_dev, t_e2e, t_main],
                                                                        [converged, flips], "cuda")
+    if dist is not None:
+        dist.destroy_process_group()
     if rank != 0:
         return None
+    # the single-GPU comparison arms and legs run at N = 1 only (the CPU
+    # baseline is a rank-0, N = 1 figure; at N > 1 they would hold every GPU)
+    single = ws == 1
     peaks, peak_kind = measured_peaks()
     achieved = BYTES_PER_FLIP * flips / max(t_main, 1e-12) / 1e9
-    plain_pps, plain_s, plain_launches = plain_run()
-    ref_cuda = reference_cuda_run()
-    cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1)
+    plain_pps, plain_s, plain_launches = plain_run() if single else (None, None, None)
+    ref_cuda = reference_cuda_run() if single else None
+    cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1) if single else (None, None, 0.0)
     line = {
         "metric": METRIC,
         "value": converged / t_dev,
@@ -477,7 +482,10 @@ def run_ours(args):
                                           "advances, so it runs without replica exchange at -c 20"}
     if clocks is not None:
         line["clocks"] = clocks
-    if not args.no_extra:
+    if not single:
+        for k in ("cpu_baseline", "plain", "accuracy"):
+            line.pop(k, None)
+    if not args.no_extra and single:
         line["batched"] = batched_run()
         line["large"] = large_run()
         line["serving"] = serving_run()
