@@ -199,9 +199,12 @@ typedef struct {
 typedef struct wlg_context wlg_context;
 
 /* A context owns a CUDA stream and the device buffers of the engine on
- * `device`.  mem_budget_bytes = 0 means no limit beyond the device's.  A
- * context serves one host thread at a time (calls on it must not overlap);
- * use one context per thread for concurrent solves. */
+ * `device`, four auxiliary streams on which a batch's launch groups (by
+ * kernel form and team size) run side by side, joined back to the solve's
+ * stream by events, and host worker threads for the per-problem host phases
+ * (started on first use).  mem_budget_bytes = 0 means no limit beyond the
+ * device's.  A context serves one host thread at a time (calls on it must
+ * not overlap); use one context per thread for concurrent solves. */
 wlg_status wlg_context_create(int device, size_t mem_budget_bytes, wlg_context** out);
 wlg_status wlg_context_destroy(wlg_context* ctx);
 /* Text of the last failure on ctx; valid until the next call on ctx. */
