@@ -266,7 +266,35 @@ def batched_run():
                         "I = N/8 in [8,32], W=4, o=0.25, alpha=0.8, ln f 1e-6, exchange every 10",
             "value": counts.get("0", 0) / dev_s, "unit": "samples/s", "e2e_samples_per_s": counts.get("0", 0) / wall,
             "status_counts": counts, "flips_per_s": flips / (st["main_ms"] / 1e3), "pre_ms": st["pre_ms"],
-            "main_ms": st["main_ms"], "main_forms": st["main_forms"], "kernel_launches": st["kernel_launches"]}
+            "main_ms": st["main_ms"], "main_forms": st["main_forms"], "kernel_launches": st["kernel_launches"],
+            "accuracy": batched_accuracy(probs, out)}
+
+
+BATCHED_ACCURACY_PER_SIDE = 4
+
+
+def batched_accuracy(probs, out):
+    """log g error of the batched leg's own output against the exact density
+    of states (transfer matrix, up to 2^100 states) for the first converged
+    samples of each side up to 10: RMS and max |log g - log g_exact| after
+    normalisation, per side."""
+    import oracle as O
+    res = {}
+    for L in (4, 6, 8, 10):
+        errs, same = [], True
+        for p, (r, E, G) in zip(probs, out):
+            if p.X != L or r.status != 0 or len(errs) == BATCHED_ACCURACY_PER_SIDE:
+                continue
+            N = L * L
+            J = O.init_interactions(L, L, p.sample + 1, p.seed, p.prob, p.error_class.decode())[p.sample * 2 * N:]
+            cnt = O.exact_counts(J, L, L, p.boundary)
+            same &= set(E.tolist()) == set((np.nonzero(cnt)[0] - 2 * N).tolist())
+            err = G - np.log(cnt[E + 2 * N])
+            errs.append((float(np.sqrt(np.mean(err ** 2))), float(np.abs(err).max())))
+        if errs:
+            res[f"{L}x{L}"] = {"curves": len(errs), "rms_mean": float(np.mean([a for a, _ in errs])),
+                               "max_abs": float(max(b for _, b in errs)), "energy_sets_exact": bool(same)}
+    return res
 
 
 LARGE = dict(sides=(16, 24), samples=38, prob=0.10, seed=4242, max_outer=10)

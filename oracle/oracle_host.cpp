@@ -512,29 +512,49 @@ int orc_stitch(const double* logG, const int* start, const int* end, int n_int, 
 // Exact number of states per energy, E in [-2N, 2N], of one coupling set
 // (reference layout), by a site-by-site transfer matrix over a front of Y
 // spins with the first row fixed (needed for the periodic wrap).  counts[]
-// has 4N+1 entries; values are exact up to 2^53.
-void orc_exact_counts(const int8_t* J, int X, int Y, int boundary, double* counts)
+// has 4N+1 entries; values are exact up to 2^53 and within one rounding of
+// the count beyond.
+//
+// Three savings that leave the counts unchanged: flipping every spin maps
+// the states with first row r0 onto those with first row ~r0 at the same
+// energy, so only first rows with spin Y-1 up are walked and the total is
+// doubled; a partial energy made of b bond terms (each +-1) lies in [-b, b]
+// with the parity of b, so only those bins are visited; and first rows are
+// split into fixed blocks of kRowsPerBlock, walked by all host threads,
+// each block summed in row order and the blocks summed in block order, so
+// the result does not depend on the number of threads.
+namespace {
+
+constexpr size_t kRowsPerBlock = 8;
+
+void exact_counts_rows(const int8_t* J, int X, int Y, int boundary, size_t r_begin, size_t r_end,
+                       std::vector<double>& cur, std::vector<double>& nxt, double* out)
 {
   const int N = X * Y;
   const int off = 2 * N;
   const int L = 4 * N + 1;
   const size_t S = static_cast<size_t>(1) << Y;
-  std::fill(counts, counts + L, 0.0);
   auto spin = [](size_t cfg, int j) { return ((cfg >> j) & 1) ? -1 : 1; };
   auto Jr = [&](int i, int j) { return static_cast<int>(J[i * Y + j]); };
   auto Jd = [&](int i, int j) { return static_cast<int>(J[N + i * Y + j]); };
-  std::vector<double> cur(S * L), nxt(S * L);
-  for (size_t r0 = 0; r0 < S; ++r0) {
-    std::fill(cur.begin(), cur.end(), 0.0);
-    int e0 = 0;
+  for (size_t r0 = r_begin; r0 < r_end; ++r0) {
+    int e0 = 0, b = 0;  // energy and bond terms of row 0
     for (int j = 0; j < Y; ++j) {
-      if (j + 1 < Y) e0 -= Jr(0, j) * spin(r0, j) * spin(r0, j + 1);
-      else if (boundary == 0) e0 -= Jr(0, j) * spin(r0, j) * spin(r0, 0);
+      if (j + 1 < Y) {
+        e0 -= Jr(0, j) * spin(r0, j) * spin(r0, j + 1);
+        ++b;
+      } else if (boundary == 0) {
+        e0 -= Jr(0, j) * spin(r0, j) * spin(r0, 0);
+        ++b;
+      }
     }
+    for (size_t f = 0; f < S; ++f) std::fill(&cur[f * L + off - b], &cur[f * L + off + b] + 1, 0.0);
     cur[r0 * L + (e0 + off)] = 1.0;
     for (int i = 1; i < X; ++i) {
       for (int j = 0; j < Y; ++j) {
-        std::fill(nxt.begin(), nxt.end(), 0.0);
+        // terms added with spin (i, j): up, left, right wrap, down wrap
+        const int nb = b + 1 + (j > 0) + (j == Y - 1 && boundary == 0) + (i == X - 1 && boundary == 0);
+        for (size_t f = 0; f < S; ++f) std::fill(&nxt[f * L + off - nb], &nxt[f * L + off + nb] + 1, 0.0);
         for (size_t f = 0; f < S; ++f) {
           const double* src = &cur[f * L];
           for (int sv = 0; sv < 2; ++sv) {
@@ -546,20 +566,49 @@ void orc_exact_counts(const int8_t* J, int X, int Y, int boundary, double* count
             }
             if (i == X - 1 && boundary == 0) de -= Jd(i, j) * s * spin(r0, j);  // down wrap to row 0
             const size_t g = (f & ~(static_cast<size_t>(1) << j)) | (static_cast<size_t>(sv) << j);
-            double* dst = &nxt[g * L];
-            for (int e = 0; e < L; ++e) {
-              if (src[e] == 0.0) continue;
-              const int en = e + de;
-              if (en >= 0 && en < L) dst[en] += src[e];
+            double* dst = &nxt[g * L + de];
+            // |e - off| <= b < nb <= 2N = off, so e + de stays in [0, L)
+            for (int e = off - b; e <= off + b; e += 2) {
+              const double v = src[e];
+              if (v != 0.0) dst[e] += v;
             }
           }
         }
         std::swap(cur, nxt);
+        b = nb;
       }
     }
     for (size_t f = 0; f < S; ++f)
-      for (int e = 0; e < L; ++e) counts[e] += cur[f * L + e];
+      for (int e = off - b; e <= off + b; e += 2) out[e] += cur[f * L + e];
   }
+}
+
+}  // namespace
+
+void orc_exact_counts(const int8_t* J, int X, int Y, int boundary, double* counts)
+{
+  const int N = X * Y;
+  const size_t L = static_cast<size_t>(4 * N + 1);
+  const size_t S = static_cast<size_t>(1) << Y;
+  const size_t rows = S / 2;  // first rows with spin Y-1 up
+  const size_t blocks = (rows + kRowsPerBlock - 1) / kRowsPerBlock;
+  std::vector<double> part(blocks * L, 0.0);
+  std::atomic<size_t> next{0};
+  auto work = [&] {
+    std::vector<double> cur(S * L), nxt(S * L);
+    for (size_t k; (k = next.fetch_add(1)) < blocks;)
+      exact_counts_rows(J, X, Y, boundary, k * kRowsPerBlock, std::min(rows, (k + 1) * kRowsPerBlock), cur, nxt,
+                        &part[k * L]);
+  };
+  const size_t threads = std::min<size_t>(blocks, std::max(1u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < threads; ++t) pool.emplace_back(work);
+  work();
+  for (std::thread& t : pool) t.join();
+  std::fill(counts, counts + L, 0.0);
+  for (size_t k = 0; k < blocks; ++k)
+    for (size_t e = 0; e < L; ++e) counts[e] += part[k * L + e];
+  for (size_t e = 0; e < L; ++e) counts[e] *= 2.0;
 }
 
 // Brute-force enumeration of the same counts (small N), a check on the

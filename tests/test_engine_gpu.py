@@ -358,6 +358,44 @@ def test_engine_8x8_log_g_and_class_probabilities_against_exact(cuda, boundary):
     assert np.abs(np.exp(lp) - np.exp(exact_lp)).max() < 0.05
 
 
+def test_engine_10x10_against_exact_and_oracle(cuda):
+    """10x10 (2^100 states, two 64-bit words of spins per walker), periodic
+    and open, all four classes in one batch: every stitched curve has exactly
+    the reachable energies and WL-size errors against the transfer matrix,
+    the class probabilities match the exact ones (on the open lattice every
+    class is a gauge copy of i: exactly 1/4 each), and the periodic class-i
+    run equals the oracle's bit for bit."""
+    import qec_pf_wang_landau_gb300 as wlg
+    X = Y = 10
+    N = X * Y
+    kw = dict(prob=0.08, seed=31, sample=0, pre_walkers=128, pre_intervals=32, pre_iterations=10000, intervals=12,
+              walkers_per_interval=4, overlap=0.25, alpha=0.8, beta=1e-4, iterations=1000, exchange_every=5)
+    probs = [wlg.problem(X, Y, boundary=b, error_class=c, **kw) for b in (0, 1) for c in "ivhc"]
+    out = wlg.Context(0).solve(probs)
+    assert all(r.status == 0 for r, _, _ in out)
+    bn = 0.5 * np.log(0.92 / 0.08)
+    for b in (0, 1):
+        exact_lz = []
+        for ci, c in enumerate("ivhc"):
+            _, E, G = out[4 * b + ci]
+            cnt = O.exact_counts(O.init_interactions(X, Y, 1, 31, 0.08, c), X, Y, b)
+            Ee = np.nonzero(cnt)[0] - 2 * N
+            assert set(E.tolist()) == set(Ee.tolist())
+            err = G - np.log(cnt[E + 2 * N])
+            assert np.sqrt(np.mean(err ** 2)) < 0.3 and np.abs(err).max() < 0.8
+            exact_lz.append(np.logaddexp.reduce(np.log(cnt[Ee + 2 * N]) - bn * Ee))
+        exact_lp = np.array(exact_lz) - np.logaddexp.reduce(exact_lz)
+        if b == 1:
+            assert np.allclose(np.exp(exact_lp), 0.25, atol=1e-12)
+        _, lp = wlg.class_log_probs([(E, G) for _, E, G in out[4 * b:4 * b + 4]], 0.08)
+        assert np.abs(np.exp(lp) - np.exp(exact_lp)).max() < 0.05
+    ref = oracle_run(X, Y, 0, 0.08, "i", 31, 1, 128, 32, 10000, 12, 4, 0.25, 0.8, 1e-4, 1000, 5, 1, 0)
+    rc, Er, Gr = O.stitch(ref["logG"], ref["start"], ref["end"], 12, 4, X, Y)
+    assert ref["status"] == 0 and rc == 0
+    _, E, G = out[0]
+    assert np.array_equal(E, Er) and np.array_equal(G, Gr)
+
+
 def test_class_log_probs_normalised(cuda):
     import qec_pf_wang_landau_gb300 as wlg
     probs = [wlg.problem(4, 4, prob=0.1, error_class=c, seed=77, sample=0, pre_walkers=32, pre_intervals=8,

@@ -80,9 +80,32 @@ def test_flip_ratio():
 @pytest.mark.parametrize("boundary", [0, 1])
 def test_transfer_matrix_equals_enumeration(boundary):
     for seed in (1, 2, 3):
-        for X, Y in ((4, 4), (3, 5), (2, 6)):
+        for X, Y in ((4, 4), (3, 5), (2, 6), (4, 5), (5, 4), (2, 2)):
             J = O.init_interactions(X, Y, 1, seed, 0.3)
             assert np.array_equal(O.exact_counts(J, X, Y, boundary), O.exact_counts(J, X, Y, boundary, brute=True))
+
+
+def test_transfer_matrix_10x10_known_answers():
+    """10x10 (2^100 states).  The ferromagnet by its low-temperature
+    expansion, each count x2 for the global flip.  Periodic: 1 ground state;
+    N single flips at -2N + 8; 2N adjacent pairs at -2N + 12; at -2N + 16,
+    C(N,2) - 2N separated pairs, 2N straight and 4N bent triples and N 2x2
+    squares.  Open (180 bonds): 4 corner flips at -180 + 4; 32 edge flips
+    and 8 corner-edge pairs at -180 + 6.  Random couplings: 2^N states in
+    all, and g(E) = g(-E) since both lattices are bipartite (the staggered
+    spin flip negates every bond term)."""
+    N = 100
+    c = O.exact_counts(np.ones(2 * N, np.int8), 10, 10, 0)
+    low = {-200: 2, -192: 2 * N, -188: 4 * N, -184: 2 * (N * (N - 1) // 2 - 2 * N + 2 * N + 4 * N + N)}
+    assert {e: c[e + 2 * N] for e in low} == low and c[-196 + 2 * N] == 0 and c[2 * N + 200] == 2
+    c = O.exact_counts(np.ones(2 * N, np.int8), 10, 10, 1)
+    assert c[-180 + 2 * N] == 2 and c[-176 + 2 * N] == 8 and c[-174 + 2 * N] == 2 * (32 + 8)
+    assert np.count_nonzero(c[:-180 + 2 * N]) == 0
+    for boundary in (0, 1):
+        J = O.init_interactions(10, 10, 1, 3, 0.2, "c")
+        c = O.exact_counts(J, 10, 10, boundary)
+        assert abs(c.sum() / 2.0 ** N - 1) < 1e-13
+        assert np.allclose(c, c[::-1], rtol=1e-13, atol=0)
 
 
 def test_p0_reachable_energies_4x4():
