@@ -510,6 +510,8 @@ def run_ours(args):
                                           "advances, so it runs without replica exchange at -c 20"}
     if clocks is not None:
         line["clocks"] = clocks
+    if single:
+        line.update(secondary_ceilings(achieved, flips / t_main))
     if not single:
         for k in ("cpu_baseline", "plain", "accuracy"):
             line.pop(k, None)
@@ -518,6 +520,24 @@ def run_ours(args):
         line["large"] = large_run()
         line["serving"] = serving_run()
     return line
+
+
+def secondary_ceilings(achieved_gbs, flips_per_s):
+    """The rates the WL step depends on besides HBM, measured on this device
+    after the timed region (wlg_measure_peaks): the main run's 34 B per flip
+    against shared-memory bandwidth (the level that holds its walker state),
+    and the step rates that Philox draws (two per step) and FP64 exp + log
+    (one each per step in the reference's formulation) would allow alone."""
+    import qec_pf_wang_landau_gb300 as wlg
+    pk = wlg.measure_peaks(0)
+    fp64_step = 1.0 / (1.0 / pk["exp_f64_per_s"] + 1.0 / pk["log_f64_per_s"])
+    return {
+        "roofline_smem": {"achieved": achieved_gbs, "peak": pk["smem_gbs"], "unit": "GB/s",
+                          "frac": achieved_gbs / pk["smem_gbs"], "peak_kind": "measured (wlg_measure_peaks)"},
+        "secondary_peaks": {**pk, "philox_step_ceiling_flips_per_s": pk["philox_draws_per_s"] / 2.0,
+                            "fp64_exp_log_step_ceiling_flips_per_s": fp64_step,
+                            "achieved_flips_per_s": flips_per_s},
+    }
 
 
 def run_reference(args):
@@ -599,7 +619,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--profile-case", default=None, help="run a small fixed case for a profiler and exit")
-    ap.add_argument("--leg", default=None, choices=["serving", "batched", "large"],
+    ap.add_argument("--leg", default=None, choices=["serving", "batched", "large", "peaks"],
                     help="run one extra leg alone and print it")
     ap.add_argument("--no-extra", action="store_true", help="skip the serving and batched legs")
     args = ap.parse_args()
@@ -609,7 +629,8 @@ def main():
     if args.leg is not None:
         import qec_pf_wang_landau_gb300 as wlg
         wlg.build()
-        legs = {"serving": serving_run, "batched": batched_run, "large": large_run}
+        legs = {"serving": serving_run, "batched": batched_run, "large": large_run,
+                "peaks": lambda: wlg.measure_peaks(0)}
         print(json.dumps({args.leg: legs[args.leg]()}), flush=True)
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -363,6 +363,24 @@ typedef struct {
 
 wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out);
 
+/* Secondary ceilings of the WL step on a device, measured by
+ * microbenchmarks that fill every SM (no counterpart in the reference;
+ * the rates its step depends on): shared-memory load bandwidth (128-bit,
+ * conflict-free), Philox4x32-10 draws (the reference's cuRAND generator,
+ * wl.cu:1074/:1114/:1167) and FP64 exp and log evaluations (its acceptance
+ * exp, wl.cu:1113-1116, and factor log, wl.cu:1124), each the fastest of
+ * three launches.  Takes a few tens of milliseconds; the calling thread's
+ * current device is restored. */
+typedef struct {
+  int sm_count;
+  double smem_gbs;           /* GB/s over the whole device */
+  double philox_draws_per_s; /* 32-bit draws per second (four per Philox block) */
+  double exp_f64_per_s;
+  double log_f64_per_s;
+} wlg_peaks;
+
+wlg_status wlg_measure_peaks(int device, wlg_peaks* out);
+
 /* Logical-class log-probabilities at the Nishimori temperature
  * beta_N = ln((1-p)/p) / 2 (no counterpart in the reference): for each of
  * n_classes normalised log g curves (energies[i], log_g[i]) with

@@ -52,6 +52,7 @@ SIGNATURES = {
     "wlg_couplings_from_syndrome": [i32, i32, i32, P, P],
     "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
     "wlg_last_stats": [P, P],
+    "wlg_measure_peaks": [i32, P],
     "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
     "wlg_solve_raw_noalloc": [P, i32, P, P, P, P, i64, P, P],
     "wlg_class_log_probs": [P, P, P, P, i32, f64, P, P],
@@ -286,6 +287,18 @@ class Tuning(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("pre_ms", f64), ("handoff_ms", f64), ("main_ms", f64), ("stitch_ms", f64), ("h2d_bytes", i64),
                 ("d2h_bytes", i64), ("kernel_launches", i32), ("main_forms", i32)]
+
+
+class Peaks(C.Structure):
+    _fields_ = [("sm_count", i32), ("smem_gbs", f64), ("philox_draws_per_s", f64), ("exp_f64_per_s", f64),
+                ("log_f64_per_s", f64)]
+
+
+def measure_peaks(device: int = 0):
+    """Secondary ceilings of the WL step measured on the device (wlg_measure_peaks)."""
+    pk = Peaks()
+    call("wlg_measure_peaks", device, C.byref(pk))
+    return {f: getattr(pk, f) for f, _ in Peaks._fields_}
 
 
 def solve_plain(problems, stream=None):

@@ -492,3 +492,20 @@ def test_check_finished_reference_cases(cuda, case):
         assert (got[:-1] == -1).all() and got[-1] == I - 1
     else:
         assert (got == 0).all()
+
+
+def test_measure_peaks(cuda):
+    """wlg_measure_peaks: every rate positive and finite, the SM count the
+    device's, shared-memory bandwidth above a plain HBM copy's order of
+    magnitude and Philox well above a draw per flip of the engine; a null
+    output is rejected and the current device is left as it was."""
+    torch = cuda
+    import qec_pf_wang_landau_gb300 as wlg
+    before = torch.cuda.current_device()
+    pk = wlg.measure_peaks(0)
+    assert torch.cuda.current_device() == before
+    assert pk["sm_count"] == torch.cuda.get_device_properties(0).multi_processor_count
+    for k in ("smem_gbs", "philox_draws_per_s", "exp_f64_per_s", "log_f64_per_s"):
+        assert np.isfinite(pk[k]) and pk[k] > 0, k
+    assert pk["smem_gbs"] > 1000.0 and pk["philox_draws_per_s"] > 1e10
+    assert wlg.lib().wlg_measure_peaks(0, None) == 1  # WLG_ERR_INVALID
