@@ -132,6 +132,47 @@ def test_mainrun_reads_a_prerun_file_in_libhdf5_default_structure(cuda, tmp_path
         assert np.array_equal(kv["Key"], E) and np.array_equal(kv["Value"], G)
 
 
+def test_programs_on_an_open_lattice(cuda, tmp_path):
+    """--boundary 1 on both programs: the files go under .../open/... (utils.cpp:88-128), the pre-run file
+    holds the oracle's open-boundary pre-run, and the main-run file the batch engine's open-boundary log g."""
+    import qec_pf_wang_landau_gb300 as wlg
+    Xo, Yo = 5, 4
+    pre = [a for a in PRE]
+    main = [a for a in MAIN]
+    for lst in (pre, main):
+        lst[lst.index("-x") + 1], lst[lst.index("-y") + 1] = str(Xo), str(Yo)
+        lst += ["--boundary", "1"]
+    assert run("wlg_prerun", pre, tmp_path).returncode == 0
+    sub = f"task_id_7/seed_{SEED}/open/prob_0.040000/X_{Xo}_Y_{Yo}/error_class_i"
+    path = str(tmp_path / "init" / sub / "prerun_results.h5")
+    N = Xo * Yo
+    seen = np.zeros(R * (4 * N + 1), np.uint8)
+    J = np.zeros(R * 2 * N, np.int8)
+    flat = np.zeros(R * 8 * N, np.int8)
+    flag = np.zeros(R * 8, np.int32)
+    en = np.zeros(R * 8, np.int32)
+    O.lib().orc_prerun(Xo, Yo, 1, C.c_float(P), b"i", SEED, R, 32, 8, 1000, O.ptr(seen), O.ptr(J), O.ptr(flat),
+                       O.ptr(flag), O.ptr(en))
+    for k in range(R):
+        assert np.array_equal(wlg.h5_read(path, f"Histogram/{k}/Histogram"), seen[k * (4 * N + 1):(k + 1) * (4 * N + 1)])
+        assert np.array_equal(wlg.h5_read(path, f"Interaction/{k}/Interaction"), J[k * 2 * N:(k + 1) * 2 * N])
+    r = run("wlg_mainrun", main + ["--exchange-mode", "1"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    out = str(tmp_path / "results" / sub / "mainrun_results.h5")
+    probs = [wlg.problem(Xo, Yo, boundary=1, prob=P, error_class="i", seed=SEED, sample=k, pre_walkers=32,
+                         pre_intervals=8, pre_iterations=1000, intervals=10, walkers_per_interval=3, overlap=0.25,
+                         alpha=0.8, beta=0.001, iterations=1000, exchange_every=20, exchange_mode=1, global_parity=1)
+             for k in range(R)]
+    ref = wlg.Context(0).solve(probs)
+    samples = sorted(int(g) for g in wlg.h5_list(out)[0])
+    assert samples == [k for k, (res, _, _) in enumerate(ref) if res.status == 0] and samples
+    for k in samples:
+        (stamp,), _ = wlg.h5_list(out, f"{k}/{SEED}")
+        kv = wlg.h5_read(out, f"{k}/{SEED}/{stamp}/log_g")
+        _, E, G = ref[k]
+        assert np.array_equal(kv["Key"], E) and np.array_equal(kv["Value"], G)
+
+
 def test_mainrun_time_limit_and_flags(cuda, tmp_path):
     assert run("wlg_prerun", PRE, tmp_path).returncode == 0
     # -f 0: the run stops at the first check; no sample converges, nothing is written
