@@ -119,46 +119,77 @@ def reference_cuda_run():
 ACCURACY_SAMPLES = 8
 
 
+def _reference_curve(run, k, X, Y, I):
+    """Stitched, normalised walker-0 log g of sample k from a run of the
+    reference's kernels, or None."""
+    import ctypes as C
+    import oracle as O
+    if run is None or run["status"] != 0:
+        return None
+    N = X * Y
+    flat = np.concatenate(run["windows"][k * I:(k + 1) * I])
+    Er = np.zeros(4 * N + 1, np.int32)
+    Gr = np.zeros(4 * N + 1)
+    n = C.c_int(0)
+    rc = O.lib().orc_stitch(O.ptr(np.ascontiguousarray(flat)), O.ptr(np.ascontiguousarray(run["start"][k * I:])),
+                            O.ptr(np.ascontiguousarray(run["end"][k * I:])), I, 1, X, Y, O.ptr(Er), O.ptr(Gr), len(Er),
+                            C.byref(n), 0)
+    return (Er[:n.value], Gr[:n.value]) if rc == 0 else None
+
+
 def accuracy(out, ref_runs):
     """log g error after normalisation against the exact density of states
     (transfer matrix over all 2^36 states) for samples 0-7 of every class:
     RMS and max |log g - log g_exact| per curve, this engine's (from the timed
-    run's own output) and the reference kernels'."""
-    import ctypes as C
+    run's own output) and the reference kernels'.  And the logical-class
+    decision of every sample (argmax over classes of log Z_c =
+    logsumexp(log g_c(E) - beta_N E) at the Nishimori temperature), compared
+    between the engine, the reference's kernels and the exact counts."""
     import oracle as O
     w = WORKLOAD
-    X, Y, N = w["X"], w["Y"], w["X"] * w["Y"]
+    X, Y, N, I = w["X"], w["Y"], w["X"] * w["Y"], w["intervals"]
+    classes = w["classes"]
+    bn = 0.5 * np.log((1.0 - w["prob"]) / w["prob"])
     res = {"engine": [], "reference_cuda": []}
     same_sets = True
-    for ci, c in enumerate(w["classes"]):
-        J = O.init_interactions(X, Y, ACCURACY_SAMPLES, w["seed"], w["prob"], c)
-        for k in range(ACCURACY_SAMPLES):
-            cnt = O.exact_counts(J[k * 2 * N:(k + 1) * 2 * N], X, Y, w["boundary"])
-            r, E, G = out[k * len(w["classes"]) + ci]
+    Js = {c: O.init_interactions(X, Y, w["samples"], w["seed"], w["prob"], c) for c in classes}
+    decisions = {"engine": [], "reference_cuda": [], "exact": []}
+    for k in range(w["samples"]):
+        lz = {key: [] for key in decisions}
+        for ci, c in enumerate(classes):
+            cnt = O.exact_counts(Js[c][k * 2 * N:(k + 1) * 2 * N], X, Y, w["boundary"])
+            Ee = np.nonzero(cnt)[0] - 2 * N
+            lz["exact"].append(np.logaddexp.reduce(np.log(cnt[Ee + 2 * N]) - bn * Ee))
+            r, E, G = out[k * len(classes) + ci]
+            lz["engine"].append(np.logaddexp.reduce(G - bn * E) if r.status == 0 else np.nan)
+            ref = _reference_curve(None if ref_runs is None else ref_runs.get(c), k, X, Y, I)
+            lz["reference_cuda"].append(np.logaddexp.reduce(ref[1] - bn * ref[0]) if ref is not None else np.nan)
+            if k >= ACCURACY_SAMPLES:
+                continue
             if r.status == 0:
-                same_sets &= set(E.tolist()) == set((np.nonzero(cnt)[0] - 2 * N).tolist())
+                same_sets &= set(E.tolist()) == set(Ee.tolist())
                 err = G - np.log(cnt[E + 2 * N])
                 res["engine"].append((float(np.sqrt(np.mean(err ** 2))), float(np.abs(err).max())))
-            run = None if ref_runs is None else ref_runs.get(c)
-            if run is not None and run["status"] == 0:
-                I = w["intervals"]
-                flat = np.concatenate(run["windows"][k * I:(k + 1) * I])
-                Er = np.zeros(4 * N + 1, np.int32)
-                Gr = np.zeros(4 * N + 1)
-                n = C.c_int(0)
-                rc = O.lib().orc_stitch(O.ptr(np.ascontiguousarray(flat)), O.ptr(np.ascontiguousarray(run["start"][k * I:])),
-                                        O.ptr(np.ascontiguousarray(run["end"][k * I:])), I, 1, X, Y, O.ptr(Er),
-                                        O.ptr(Gr), len(Er), C.byref(n), 0)
-                if rc == 0:
-                    e = Gr[:n.value] - np.log(cnt[Er[:n.value] + 2 * N])
-                    res["reference_cuda"].append((float(np.sqrt(np.mean(e ** 2))), float(np.abs(e).max())))
-    summary = {"curves": f"samples 0-{ACCURACY_SAMPLES - 1} x classes {w['classes']}",
+            if ref is not None:
+                e = ref[1] - np.log(cnt[ref[0] + 2 * N])
+                res["reference_cuda"].append((float(np.sqrt(np.mean(e ** 2))), float(np.abs(e).max())))
+        for key, v in lz.items():
+            decisions[key].append(int(np.argmax(v)) if np.all(np.isfinite(v)) else -1)
+    summary = {"curves": f"samples 0-{ACCURACY_SAMPLES - 1} x classes {classes}",
                "exact": "transfer-matrix density of states over all 2^36 states",
                "engine_energy_sets_exact": bool(same_sets)}
     for key, v in res.items():
         if v:
             summary[key] = {"rms_mean": float(np.mean([a for a, _ in v])), "max_abs": float(max(b for _, b in v)),
                             "curves": len(v)}
+    d = {key: np.array(v) for key, v in decisions.items()}
+    summary["class_decisions"] = {
+        "samples": w["samples"],
+        "engine_equals_exact": int(np.sum((d["engine"] == d["exact"]) & (d["engine"] >= 0))),
+        "engine_equals_reference_cuda": int(np.sum((d["engine"] == d["reference_cuda"]) & (d["engine"] >= 0))),
+        "reference_cuda_equals_exact": int(np.sum((d["reference_cuda"] == d["exact"]) & (d["reference_cuda"] >= 0))),
+        "exact_classes": {c: int(np.sum(d["exact"] == ci)) for ci, c in enumerate(classes)},
+    }
     return summary
 
 
