@@ -43,3 +43,28 @@ def test_batched_workload():
     assert {p.boundary for p in probs} == {0, 1}
     assert {p.error_class for p in probs} == {b"i", b"v", b"h", b"c"}
     assert all(8 <= p.intervals <= 32 and p.walkers_per_interval == 4 and p.beta == 1e-6 for p in probs)
+
+
+def test_accuracy_scores_exact_curves_as_exact():
+    """The accuracy leg on curves that are the exact log g themselves (shifted
+    by a constant, as a normalisation error would): zero RMS after the
+    shift's own size, energy sets exact, every class decision equal to the
+    exact one; a failed problem leaves its sample out of the decisions."""
+    import types
+    import bench
+    import oracle as O
+    w = bench.WORKLOAD
+    N = w["X"] * w["Y"]
+    out = []
+    Js = {c: O.init_interactions(w["X"], w["Y"], w["samples"], w["seed"], w["prob"], c) for c in w["classes"]}
+    for k in range(w["samples"]):
+        for c in w["classes"]:
+            cnt = O.exact_counts(Js[c][k * 2 * N:(k + 1) * 2 * N], w["X"], w["Y"], w["boundary"])
+            E = (np.nonzero(cnt)[0] - 2 * N).astype(np.int32)
+            out.append((types.SimpleNamespace(status=0), E, np.log(cnt[E + 2 * N]) + 1e-3))
+    out[5] = (types.SimpleNamespace(status=3), np.zeros(0, np.int32), np.zeros(0))  # sample 1, class v
+    acc = bench.accuracy(out, None)
+    assert acc["engine_energy_sets_exact"] and abs(acc["engine"]["rms_mean"] - 1e-3) < 1e-9
+    d = acc["class_decisions"]
+    assert d["samples"] == 100 and d["engine_equals_exact"] == 99 and d["reference_cuda_equals_exact"] == 0
+    assert sum(d["exact_classes"].values()) == 100
