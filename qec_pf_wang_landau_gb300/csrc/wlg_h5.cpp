@@ -9,6 +9,7 @@
 
 #include "wlg_h5.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -411,27 +412,40 @@ struct In {
   bool ok = true;
   bool need(uint64_t n)
   {
-    if (pos + n > b.size()) ok = false;
+    if (n > b.size() || pos > b.size() - n) ok = false;  // no wrap-around for offsets read from the file
     return ok;
   }
+  // Little-endian field of n <= 8 bytes (field sizes can come from the file).
   uint64_t le(int n)
   {
-    if (!need(static_cast<uint64_t>(n))) return 0;
+    if (n < 0 || n > 8) ok = false;
+    if (!ok || !need(static_cast<uint64_t>(n))) return 0;
     uint64_t v = 0;
     for (int i = 0; i < n; ++i) v |= static_cast<uint64_t>(b[pos + i]) << (8 * i);
     pos += static_cast<uint64_t>(n);
     return v;
   }
+  void skip(uint64_t n)
+  {
+    if (need(n)) pos += n;
+  }
 };
 
+// [at, at + n) lies inside the file (no wrap-around for file offsets).
+bool fits(const std::vector<uint8_t>& file, uint64_t at, uint64_t n)
+{
+  return n <= file.size() && at <= file.size() - n;
+}
+
 // Datatype at in.pos -> Type; false if not one this module writes.
-bool parse_type(In& in, Type& t)
+bool parse_type(In& in, Type& t, bool member = false)
 {
   const uint64_t start = in.pos;
   const unsigned cv = static_cast<unsigned>(in.le(1));
   const unsigned f0 = static_cast<unsigned>(in.le(1));
   in.le(2);
   const uint64_t size = in.le(4);
+  if (!in.ok) return false;
   const unsigned cls = cv & 0x0f;
   if (cls == 0) {
     in.le(4);
@@ -443,12 +457,12 @@ bool parse_type(In& in, Type& t)
     return in.ok;
   }
   if (cls == 1) {
-    in.le(12);
+    in.skip(12);
     if (size != 8) return false;
     t = Type::f64;
     return in.ok;
   }
-  if (cls == 6 && (cv >> 4) == 1 && size == 16) {
+  if (cls == 6 && (cv >> 4) == 1 && size == 16 && !member) {
     // version-1 compound: two members Key (int32 at 0), Value (float64 at 8)
     const unsigned members = f0 | (static_cast<unsigned>(in.b[start + 2]) << 8);
     if (members != 2) return false;
@@ -458,9 +472,9 @@ bool parse_type(In& in, Type& t)
       const size_t padded = (name.size() + 1 + 7) / 8 * 8;
       in.pos += padded - name.size();
       const uint64_t off = in.le(4);
-      in.le(28);
+      in.skip(28);
       Type mt;
-      if (!parse_type(in, mt)) return false;
+      if (!parse_type(in, mt, true)) return false;
       if (m == 0 && (name != "Key" || off != 0 || mt != Type::i32)) return false;
       if (m == 1 && (name != "Value" || off != 8 || mt != Type::f64)) return false;
     }
@@ -491,7 +505,7 @@ uint32_t le32_at(const std::vector<uint8_t>& f, uint64_t a)
 std::string header_messages(const std::vector<uint8_t>& file, uint64_t addr, std::vector<HMsg>& out)
 {
   out.clear();
-  if (addr + 16 > file.size()) return "object header address";
+  if (!fits(file, addr, 16)) return "object header address";
   std::vector<std::pair<uint64_t, uint64_t>> blocks;  // message ranges still to read
   const bool v2 = std::memcmp(file.data() + addr, "OHDR", 4) == 0;
   unsigned crt = 0;
@@ -500,12 +514,12 @@ std::string header_messages(const std::vector<uint8_t>& file, uint64_t addr, std
     const unsigned version = static_cast<unsigned>(in.le(1));
     const unsigned flags = static_cast<unsigned>(in.le(1));
     if (version != 2) return "object header version";
-    if (flags & 0x20) in.le(16);
+    if (flags & 0x20) in.skip(16);
     if (flags & 0x10) in.le(4);
     const uint64_t chunk = in.le(1 << (flags & 3));
     crt = (flags & 0x04) ? 2 : 0;
+    if (!in.ok || !fits(file, in.pos, chunk) || !fits(file, in.pos + chunk, 4)) return "object header size";
     const uint64_t msg_start = in.pos, msg_end = in.pos + chunk;
-    if (!in.ok || msg_end + 4 > file.size()) return "object header size";
     if (lookup3(file.data() + addr, msg_end - addr) != le32_at(file, msg_end)) return "object header checksum";
     blocks.emplace_back(msg_start, msg_end);
   } else {
@@ -515,7 +529,7 @@ std::string header_messages(const std::vector<uint8_t>& file, uint64_t addr, std
     in.le(2);  // message count (the blocks' sizes bound the reading)
     in.le(4);  // reference count
     const uint64_t size = in.le(4);
-    if (!in.ok || addr + 16 + size > file.size()) return "object header size";
+    if (!in.ok || !fits(file, addr + 16, size)) return "object header size";
     blocks.emplace_back(addr + 16, addr + 16 + size);
   }
   for (size_t bi = 0; bi < blocks.size(); ++bi) {
@@ -548,7 +562,7 @@ std::string header_messages(const std::vector<uint8_t>& file, uint64_t addr, std
       if (type == kContinuation) {
         In c{file, body};
         const uint64_t at = c.le(8), len = c.le(8);
-        if (!c.ok || at + len > file.size()) return "continuation address";
+        if (!c.ok || !fits(file, at, len)) return "continuation address";
         blocks.emplace_back(at, at + len);
       } else if (type != kNil) {
         out.push_back({type, body, size});
@@ -561,17 +575,25 @@ std::string header_messages(const std::vector<uint8_t>& file, uint64_t addr, std
 
 // Links of an old-style group (III.A.1 version-1 B-tree of group nodes,
 // III.B symbol table nodes, III.D local heap for the names).
+// Limits that bound the work on a damaged or hostile file (nodes shared
+// between parents, links back to an ancestor): far above what the programs
+// write (a pre-run file of 1000 samples holds ~10^5 objects).
+constexpr size_t kMaxNodes = size_t{1} << 20;
+constexpr size_t kMaxLinks = size_t{1} << 22;
+
 std::string symbol_table_links(const std::vector<uint8_t>& file, uint64_t btree, uint64_t heap,
-                               std::vector<std::pair<std::string, uint64_t>>& links, int depth)
+                               std::vector<std::pair<std::string, uint64_t>>& links, int depth, int expect_level,
+                               size_t& nodes)
 {
   if (depth > 32) return "B-tree too deep";
-  if (heap + 32 > file.size() || std::memcmp(file.data() + heap, "HEAP", 4) != 0) return "local heap";
+  if (++nodes > kMaxNodes) return "too many B-tree nodes";
+  if (!fits(file, heap, 32) || std::memcmp(file.data() + heap, "HEAP", 4) != 0) return "local heap";
   In h{file, heap + 8};
   const uint64_t seg_size = h.le(8);
   h.le(8);
   const uint64_t seg = h.le(8);
-  if (!h.ok || seg + seg_size > file.size()) return "local heap segment";
-  if (btree + 24 > file.size() || std::memcmp(file.data() + btree, "TREE", 4) != 0) return "group B-tree";
+  if (!h.ok || !fits(file, seg, seg_size)) return "local heap segment";
+  if (!fits(file, btree, 24) || std::memcmp(file.data() + btree, "TREE", 4) != 0) return "group B-tree";
   In t{file, btree + 4};
   const unsigned type = static_cast<unsigned>(t.le(1));
   const unsigned level = static_cast<unsigned>(t.le(1));
@@ -579,16 +601,17 @@ std::string symbol_table_links(const std::vector<uint8_t>& file, uint64_t btree,
   t.le(8);
   t.le(8);
   if (type != 0) return "B-tree node type";
+  if (expect_level >= 0 && static_cast<int>(level) != expect_level) return "B-tree level";
   for (uint64_t k = 0; k < used; ++k) {
     t.le(8);  // key: heap offset of the largest name in the child
     const uint64_t child = t.le(8);
     if (!t.ok) return "B-tree node";
     if (level > 0) {
-      const std::string err = symbol_table_links(file, child, heap, links, depth + 1);
+      const std::string err = symbol_table_links(file, child, heap, links, depth + 1, static_cast<int>(level) - 1, nodes);
       if (!err.empty()) return err;
       continue;
     }
-    if (child + 8 > file.size() || std::memcmp(file.data() + child, "SNOD", 4) != 0) return "symbol table node";
+    if (!fits(file, child, 8) || std::memcmp(file.data() + child, "SNOD", 4) != 0) return "symbol table node";
     In sn{file, child + 4};
     if (sn.le(1) != 1) return "symbol table node version";
     sn.le(1);
@@ -598,8 +621,9 @@ std::string symbol_table_links(const std::vector<uint8_t>& file, uint64_t btree,
       const uint64_t obj = sn.le(8);
       sn.le(4);
       sn.le(4);
-      sn.le(16);
+      sn.skip(16);
       if (!sn.ok || name_off >= seg_size) return "symbol table entry";
+      if (links.size() >= kMaxLinks) return "too many links";
       const char* nm = reinterpret_cast<const char*>(file.data() + seg + name_off);
       links.emplace_back(std::string(nm, strnlen(nm, seg_size - name_off)), obj);
     }
@@ -607,10 +631,21 @@ std::string symbol_table_links(const std::vector<uint8_t>& file, uint64_t btree,
   return "";
 }
 
+// Work bounds of one parse: every object header takes at least 16 bytes of
+// the file and every dataset's bytes are stored once, so a file whose links
+// reach more objects or more data than that shares objects between parents
+// (or links back to an ancestor) and is refused.
+struct Budget {
+  uint64_t objects, bytes;
+  std::vector<uint64_t> ancestors;
+};
+
 std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group* g, Dataset* d, int depth,
-                         bool* is_group)
+                         bool* is_group, Budget& budget)
 {
   if (depth > 64) return "nesting too deep";
+  if (budget.objects == 0) return "objects shared between groups";
+  --budget.objects;
   std::vector<HMsg> msgs;
   std::string herr = header_messages(file, addr, msgs);
   if (!herr.empty()) return herr;
@@ -643,7 +678,8 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
       case kSymbolTable: {
         const uint64_t bt = m.le(8), hp = m.le(8);
         if (!m.ok) break;
-        const std::string err = symbol_table_links(file, bt, hp, links, 0);
+        size_t nodes = 0;
+        const std::string err = symbol_table_links(file, bt, hp, links, 0, -1, nodes);
         if (!err.empty()) return err;
         break;
       }
@@ -659,7 +695,11 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
           return "dataspace version";
         }
         count = 1;
-        for (unsigned r = 0; r < rank; ++r) count *= m.le(8);
+        for (unsigned r = 0; r < rank; ++r) {
+          const uint64_t dim = m.le(8);
+          if (dim != 0 && count > ~uint64_t{0} / dim) return "dataspace size";
+          count *= dim;
+        }
         break;
       }
       case kDatatype:
@@ -694,7 +734,7 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
         m.pos += pad(nsz);
         const uint64_t dt = m.pos;
         m.pos += pad(tsz) + pad(ssz);
-        if ((file[dt] & 0x0f) == 3) {
+        if (tsz >= 8 && (file[dt] & 0x0f) == 3) {
           const uint64_t len = static_cast<uint64_t>(file[dt + 4]) | static_cast<uint64_t>(file[dt + 5]) << 8;
           if (m.need(len)) {
             std::string v(reinterpret_cast<const char*>(file.data() + m.pos), len);
@@ -715,7 +755,10 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
     d->type = type;
     d->count = count;
     d->string_attrs = attrs;
-    if (data_size != count * elem_size(type)) return "dataset size";
+    const uint64_t esize = elem_size(type);
+    if (data_size % esize != 0 || count != data_size / esize) return "dataset size";
+    if (data_size > budget.bytes) return "data shared between datasets";
+    budget.bytes -= data_size;
     if (is_compact) {
       d->bytes = compact;
     } else if (data_size > 0) {
@@ -730,7 +773,11 @@ std::string parse_object(const std::vector<uint8_t>& file, uint64_t addr, Group*
     Dataset ds;
     bool child_group = false;
     // a child is a dataset exactly when its header has a layout message
-    std::string err = parse_object(file, child, &sub, &ds, depth + 1, &child_group);
+    if (std::find(budget.ancestors.begin(), budget.ancestors.end(), child) != budget.ancestors.end())
+      return name + ": link to an enclosing group";
+    budget.ancestors.push_back(addr);
+    std::string err = parse_object(file, child, &sub, &ds, depth + 1, &child_group, budget);
+    budget.ancestors.pop_back();
     if (!err.empty()) return name + ": " + err;
     if (child_group) g->groups[name] = std::make_unique<Group>(std::move(sub));
     else g->datasets[name] = std::move(ds);
@@ -781,7 +828,8 @@ std::string read_file(const std::string& path, Group& root)
   root.datasets.clear();
   bool is_group = false;
   Dataset unused;
-  std::string err = parse_object(file, root_addr, &root, &unused, 0, &is_group);
+  Budget budget{file.size() / 16 + 1, file.size(), {}};
+  std::string err = parse_object(file, root_addr, &root, &unused, 0, &is_group, budget);
   if (err.empty() && !is_group) err = "root is not a group";
   return err;
 }
