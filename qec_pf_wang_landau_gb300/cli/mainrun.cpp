@@ -118,13 +118,20 @@ int main(int argc, char** argv)
       const wlg::h5::Dataset& jd = need("Interaction", "Interaction");
       if (jd.count != static_cast<uint64_t>(2 * N) || jd.type != wlg::h5::Type::i8)
         throw std::runtime_error("Interaction length does not coincide with length of interaction written to file");
+      auto pm1 = [](const std::vector<uint8_t>& v) {
+        return std::all_of(v.begin(), v.end(), [](uint8_t x) { return x == 0x01 || x == 0xFF; });
+      };
+      if (!pm1(jd.bytes)) throw std::runtime_error("Interaction values other than +-1");
       J.insert(J.end(), jd.bytes.begin(), jd.bytes.end());
       int stored = 0;
       auto lg = pre.groups.find("Lattice");
       if (lg != pre.groups.end() && lg->second->groups.count(key)) {
         for (const auto& [ename, eg] : lg->second->groups.at(key)->groups) {
           auto ds = eg->datasets.find("Lattice");
-          if (ds == eg->datasets.end() || ds->second.count != static_cast<uint64_t>(N)) continue;
+          if (ds == eg->datasets.end() || ds->second.count != static_cast<uint64_t>(N) ||
+              ds->second.type != wlg::h5::Type::i8)
+            continue;
+          if (!pm1(ds->second.bytes)) throw std::runtime_error("Lattice values other than +-1");
           found.push_back(1);
           energy.push_back(std::stoi(ename));
           lat.insert(lat.end(), ds->second.bytes.begin(), ds->second.bytes.end());
