@@ -1153,8 +1153,20 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
       return st;
     }
     long long ob = 0;
+    auto pm1 = [](const signed char* v, long long m) {
+      for (long long i = 0; i < m; ++i)
+        if (v[i] != 1 && v[i] != -1) return false;
+      return true;
+    };
     for (int p = 0; p < n; ++p) {
       const PreDesc& d = po.pd[p];
+      bool valid = pm1(couplings + d.off_J, 2LL * d.N);
+      for (int b = 0; b < d.n_int && valid; ++b)
+        valid = found[ob + b] == 0 || pm1(lattices + d.off_found + static_cast<long long>(b) * d.N, d.N);
+      if (!valid) {
+        ctx->err = "couplings or stored lattice of problem " + std::to_string(p) + " not +-1";
+        return WLG_ERR_INVALID;
+      }
       std::memcpy(po.seen.data() + d.off_seen, seen + d.off_seen, static_cast<size_t>(4 * d.N + 1));
       std::memcpy(po.J8.data() + d.off_J, couplings + d.off_J, static_cast<size_t>(2 * d.N));
       std::memcpy(po.found.data() + d.off_found, lattices + d.off_found, static_cast<size_t>(d.n_int) * d.N);

@@ -457,3 +457,28 @@ def test_full_bench_workload_properties(cuda):
     for k in range(100):
         _, lp = wlg.class_log_probs([(E, G) for _, E, G in out[4 * k:4 * k + 4]], 0.04)
         assert abs(np.logaddexp.reduce(lp)) < 1e-12
+
+
+@pytest.mark.parametrize("what", ["couplings", "lattice"])
+def test_mainrun_entry_refuses_values_other_than_pm1(cuda, what):
+    """wlg_mainrun (main run from pre-run data) checks the caller's couplings
+    and stored lattices before any device work: a value other than +-1 is
+    WLG_ERR_INVALID with the problem named."""
+    import qec_pf_wang_landau_gb300 as wlg
+    X = Y = 4
+    N = X * Y
+    q = wlg.problem(X, Y, pre_walkers=1, pre_intervals=1, pre_iterations=0, intervals=2, walkers_per_interval=2)
+    probs = (wlg.Problem * 1)(q)
+    seen = np.ones(4 * N + 1, np.uint8)
+    J = np.ones(2 * N, np.int8)
+    lat = -np.ones(N, np.int8)
+    (J if what == "couplings" else lat)[5] = 0
+    found = np.ones(1, np.int32)
+    energy = np.array([-2 * N], np.int32)
+    res = (wlg.Result * 1)()
+    E = np.zeros(4 * N + 1, np.int32)
+    G = np.zeros(4 * N + 1)
+    ctx = wlg.Context(0)
+    st = wlg.lib().wlg_mainrun(ctx._h, C.cast(probs, C.c_void_p), 1, O.ptr(seen), O.ptr(J), O.ptr(found),
+                               O.ptr(energy), O.ptr(lat), 60.0, C.cast(res, C.c_void_p), O.ptr(E), O.ptr(G), len(E))
+    assert st == 1 and "problem 0 not +-1" in wlg.lib().wlg_context_last_error(ctx._h).decode()
