@@ -122,3 +122,13 @@ def test_corrupted_file_rejected(engine, written, tmp_path):
     bad.write_bytes(bytes(b))
     with pytest.raises(engine.WlgError):
         engine.h5_list(str(bad))
+
+
+def test_damaged_files_fail_cleanly(engine, written, tmp_path):
+    """Damaged copies of a file in the engine's own structure (superblock 2,
+    version-2 headers, checksums): every reader call returns a status; the
+    child process neither crashes nor hangs."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import h5fuzz
+    h5fuzz.check(engine.LIB, written, tmp_path)
