@@ -62,3 +62,19 @@ def test_cpp_examples_compile_against_the_header(tmp_path):
     r = subprocess.run([cxx, "-std=c++20", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_python_example_names_exist():
+    """Every wlg.<name> the Python example uses exists in the binding, and the
+    methods it calls exist on Context and Server."""
+    import ast
+    import qec_pf_wang_landau_gb300 as wlg
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    (block,) = re.findall(r"```python\n(.*?)```", text, re.S)
+    tree = ast.parse(block)
+    for node in ast.walk(tree):
+        if isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name) and node.value.id == "wlg":
+            assert hasattr(wlg, node.attr), node.attr
+    for cls, methods in ((wlg.Context, ("solve", "set_stitching")), (wlg.Server, ("submit", "wait"))):
+        for m in methods:
+            assert callable(getattr(cls, m)), (cls.__name__, m)
