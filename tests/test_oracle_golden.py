@@ -108,6 +108,19 @@ def test_transfer_matrix_10x10_known_answers():
         assert np.allclose(c, c[::-1], rtol=1e-13, atol=0)
 
 
+def test_error_classes_are_gauge_copies_on_open_lattices_only():
+    """The class chains (prerun.cu:56-75) negate a full column of right bonds
+    (v) or a full row of down bonds (h).  On an open lattice that is a gauge
+    transformation (flip every spin of column 0 / row 0), so all four classes
+    have exactly the same density of states; on a torus the chain crosses a
+    non-contractible loop and the densities differ."""
+    for X, Y in ((6, 6), (5, 7)):
+        opn = [O.exact_counts(O.init_interactions(X, Y, 1, 9, 0.15, c), X, Y, 1) for c in "ivhc"]
+        assert all(np.array_equal(opn[0], c) for c in opn[1:])
+        per = [O.exact_counts(O.init_interactions(X, Y, 1, 9, 0.15, c), X, Y, 0) for c in "ivhc"]
+        assert not any(np.array_equal(per[0], c) for c in per[1:])
+
+
 def test_p0_reachable_energies_4x4():
     """test_wang_landau_pre_run.cu:601-815: every multiple of 4 except +-28 (periodic); open rule."""
     J = np.ones(32, np.int8)
