@@ -301,20 +301,22 @@ def batched_run():
             "accuracy": batched_accuracy(probs, out)}
 
 
-BATCHED_ACCURACY_PER_SIDE = 4
+# curves scored per side: a periodic 12x12 curve takes tens of seconds of
+# host time (2^143 states through the transfer matrix), the others well under one
+BATCHED_ACCURACY_PER_SIDE = {4: 4, 6: 4, 8: 4, 10: 4, 12: 2}
 
 
 def batched_accuracy(probs, out):
     """log g error of the batched leg's own output against the exact density
-    of states (transfer matrix, up to 2^100 states) for the first converged
-    samples of each side up to 10: RMS and max |log g - log g_exact| after
+    of states (transfer matrix, up to 2^144 states) for the first converged
+    samples of every side: RMS and max |log g - log g_exact| after
     normalisation, per side."""
     import oracle as O
     res = {}
-    for L in (4, 6, 8, 10):
+    for L, cap in BATCHED_ACCURACY_PER_SIDE.items():
         errs, same = [], True
         for p, (r, E, G) in zip(probs, out):
-            if p.X != L or r.status != 0 or len(errs) == BATCHED_ACCURACY_PER_SIDE:
+            if p.X != L or r.status != 0 or len(errs) == cap:
                 continue
             N = L * L
             J = O.init_interactions(L, L, p.sample + 1, p.seed, p.prob, p.error_class.decode())[p.sample * 2 * N:]

@@ -511,75 +511,102 @@ int orc_stitch(const double* logG, const int* start, const int* end, int n_int, 
 
 // Exact number of states per energy, E in [-2N, 2N], of one coupling set
 // (reference layout), by a site-by-site transfer matrix over a front of Y
-// spins with the first row fixed (needed for the periodic wrap).  counts[]
-// has 4N+1 entries; values are exact up to 2^53 and within one rounding of
-// the count beyond.
+// spins: adding spin (i, j) replaces spin (i-1, j) in the front.  counts[]
+// has 4N+1 entries; values are exact up to 2^53 and within rounding of the
+// count beyond.
 //
-// Three savings that leave the counts unchanged: flipping every spin maps
-// the states with first row r0 onto those with first row ~r0 at the same
-// energy, so only first rows with spin Y-1 up are walked and the total is
-// doubled; a partial energy made of b bond terms (each +-1) lies in [-b, b]
-// with the parity of b, so only those bins are visited; and first rows are
-// split into fixed blocks of kRowsPerBlock, walked by all host threads,
-// each block summed in row order and the blocks summed in block order, so
-// the result does not depend on the number of threads.
+// A partial energy made of b bond terms (each +-1) lies in [-b, b] with the
+// parity of b, so each front configuration holds b+1 bins, bin t standing
+// for energy -b + 2t, and adding a spin that brings nb - b more terms moves
+// bin t to bin t + (de + nb - b) / 2.  Each new front configuration g is
+// gathered from its two predecessors (g with spin j up, then down) in one
+// contiguous pass that vectorises: bins are stored with kPad zero slots on
+// either side, so the shifted reads never leave a front's slice.
+//
+// Periodic lattices: the down wrap of the last row needs row 0, so the first
+// row is fixed and walked over; flipping every spin maps the states with
+// first row r0 onto those with first row ~r0 at the same energy, so only
+// first rows with spin Y-1 up are walked and the total is doubled.  First
+// rows are split into fixed blocks of kRowsPerBlock, walked by all host
+// threads, each block summed in row order and the blocks summed in block
+// order, so the result does not depend on the number of threads.
+// Open lattices: no bond reaches back to row 0, so one pass starts from all
+// first rows at once.
 namespace {
 
 constexpr size_t kRowsPerBlock = 8;
+constexpr int kPad = 4;  // a spin adds at most 4 terms, so a bin moves by at most 4
 
-void exact_counts_rows(const int8_t* J, int X, int Y, int boundary, size_t r_begin, size_t r_end,
-                       std::vector<double>& cur, std::vector<double>& nxt, double* out)
-{
-  const int N = X * Y;
-  const int off = 2 * N;
-  const int L = 4 * N + 1;
-  const size_t S = static_cast<size_t>(1) << Y;
-  auto spin = [](size_t cfg, int j) { return ((cfg >> j) & 1) ? -1 : 1; };
-  auto Jr = [&](int i, int j) { return static_cast<int>(J[i * Y + j]); };
-  auto Jd = [&](int i, int j) { return static_cast<int>(J[N + i * Y + j]); };
-  for (size_t r0 = r_begin; r0 < r_end; ++r0) {
-    int e0 = 0, b = 0;  // energy and bond terms of row 0
-    for (int j = 0; j < Y; ++j) {
-      if (j + 1 < Y) {
-        e0 -= Jr(0, j) * spin(r0, j) * spin(r0, j + 1);
-        ++b;
-      } else if (boundary == 0) {
-        e0 -= Jr(0, j) * spin(r0, j) * spin(r0, 0);
-        ++b;
-      }
-    }
-    for (size_t f = 0; f < S; ++f) std::fill(&cur[f * L + off - b], &cur[f * L + off + b] + 1, 0.0);
-    cur[r0 * L + (e0 + off)] = 1.0;
+struct ExactLattice {
+  const int8_t* J;
+  int X, Y, N, boundary;
+  size_t S;      // front configurations, 2^Y
+  size_t Lc;     // slots per front configuration: kPad, 2N + 1 bins, kPad
+  static int spin(size_t cfg, int j) { return ((cfg >> j) & 1) ? -1 : 1; }
+  int Jr(int i, int j) const { return static_cast<int>(J[i * Y + j]); }
+  int Jd(int i, int j) const { return static_cast<int>(J[N + i * Y + j]); }
+
+  // bond terms and energy of a first row
+  int row0_terms() const { return boundary == 0 ? Y : Y - 1; }
+  int row0_energy(size_t r0) const
+  {
+    int e = 0;
+    for (int j = 0; j + 1 < Y; ++j) e -= Jr(0, j) * spin(r0, j) * spin(r0, j + 1);
+    if (boundary == 0) e -= Jr(0, Y - 1) * spin(r0, Y - 1) * spin(r0, 0);
+    return e;
+  }
+
+  // Rows 1..X-1 added to the fronts in cur (b terms so far); r0 is the first
+  // row for the periodic down wrap.  Returns the final number of terms.
+  int add_rows(size_t r0, int b, std::vector<double>& cur, std::vector<double>& nxt) const
+  {
     for (int i = 1; i < X; ++i) {
       for (int j = 0; j < Y; ++j) {
         // terms added with spin (i, j): up, left, right wrap, down wrap
-        const int nb = b + 1 + (j > 0) + (j == Y - 1 && boundary == 0) + (i == X - 1 && boundary == 0);
-        for (size_t f = 0; f < S; ++f) std::fill(&nxt[f * L + off - nb], &nxt[f * L + off + nb] + 1, 0.0);
-        for (size_t f = 0; f < S; ++f) {
-          const double* src = &cur[f * L];
-          for (int sv = 0; sv < 2; ++sv) {
-            const int s = sv ? -1 : 1;
-            int de = -Jd(i - 1, j) * s * spin(f, j);                 // up bond
-            if (j > 0) de -= Jr(i, j - 1) * s * spin(f, j - 1);       // left bond
-            if (j == Y - 1 && boundary == 0) {
-              de -= Jr(i, j) * s * ((j == 0) ? s : spin(f, 0));       // right wrap
-            }
-            if (i == X - 1 && boundary == 0) de -= Jd(i, j) * s * spin(r0, j);  // down wrap to row 0
-            const size_t g = (f & ~(static_cast<size_t>(1) << j)) | (static_cast<size_t>(sv) << j);
-            double* dst = &nxt[g * L + de];
-            // |e - off| <= b < nb <= 2N = off, so e + de stays in [0, L)
-            for (int e = off - b; e <= off + b; e += 2) {
-              const double v = src[e];
-              if (v != 0.0) dst[e] += v;
-            }
+        const bool rwrap = j == Y - 1 && boundary == 0, dwrap = i == X - 1 && boundary == 0;
+        const int nb = b + 1 + (j > 0) + rwrap + dwrap;
+        const size_t bit = static_cast<size_t>(1) << j;
+        for (size_t g = 0; g < S; ++g) {
+          const int s = spin(g, j);
+          const double* src[2];
+          for (int u = 0; u < 2; ++u) {
+            const size_t f = u ? (g | bit) : (g & ~bit);
+            int de = -Jd(i - 1, j) * s * spin(f, j);                        // up bond
+            if (j > 0) de -= Jr(i, j - 1) * s * spin(f, j - 1);              // left bond
+            if (rwrap) de -= Jr(i, j) * s * ((j == 0) ? s : spin(f, 0));     // right wrap
+            if (dwrap) de -= Jd(i, j) * s * spin(r0, j);                     // down wrap to row 0
+            // de has the parity of nb - b and |de| <= nb - b <= kPad: new bin t
+            // reads old bin t - (de + nb - b) / 2, in [-kPad, b + kPad]
+            src[u] = &cur[f * Lc + kPad] - (de + nb - b) / 2;
           }
+          const double* __restrict s0 = src[0];
+          const double* __restrict s1 = src[1];
+          double* __restrict d = &nxt[g * Lc + kPad];
+          for (int t = 0; t <= nb; ++t) d[t] = s0[t] + s1[t];
+          std::fill(d + nb + 1, d + nb + 1 + kPad, 0.0);  // upper pad for the next step
         }
         std::swap(cur, nxt);
         b = nb;
       }
     }
+    return b;
+  }
+
+  void accumulate(int b, const std::vector<double>& cur, double* out) const
+  {
     for (size_t f = 0; f < S; ++f)
-      for (int e = off - b; e <= off + b; e += 2) out[e] += cur[f * L + e];
+      for (int t = 0; t <= b; ++t) out[2 * N - b + 2 * t] += cur[f * Lc + kPad + t];
+  }
+};
+
+void exact_counts_rows(const ExactLattice& lat, size_t r_begin, size_t r_end, std::vector<double>& cur,
+                       std::vector<double>& nxt, double* out)
+{
+  const int b0 = lat.row0_terms();
+  for (size_t r0 = r_begin; r0 < r_end; ++r0) {
+    for (size_t f = 0; f < lat.S; ++f) std::fill(&cur[f * lat.Lc], &cur[f * lat.Lc] + b0 + 1 + 2 * kPad, 0.0);
+    cur[r0 * lat.Lc + kPad + (lat.row0_energy(r0) + b0) / 2] = 1.0;
+    lat.accumulate(lat.add_rows(r0, b0, cur, nxt), cur, out);
   }
 }
 
@@ -590,22 +617,29 @@ void orc_exact_counts(const int8_t* J, int X, int Y, int boundary, double* count
   const int N = X * Y;
   const size_t L = static_cast<size_t>(4 * N + 1);
   const size_t S = static_cast<size_t>(1) << Y;
+  const ExactLattice lat{J, X, Y, N, boundary, S, static_cast<size_t>(2 * N + 1 + 2 * kPad)};
+  std::fill(counts, counts + L, 0.0);
+  if (boundary != 0) {
+    std::vector<double> cur(S * lat.Lc, 0.0), nxt(S * lat.Lc, 0.0);
+    const int b0 = lat.row0_terms();
+    for (size_t r0 = 0; r0 < S; ++r0) cur[r0 * lat.Lc + kPad + (lat.row0_energy(r0) + b0) / 2] = 1.0;
+    lat.accumulate(lat.add_rows(0, b0, cur, nxt), cur, counts);
+    return;
+  }
   const size_t rows = S / 2;  // first rows with spin Y-1 up
   const size_t blocks = (rows + kRowsPerBlock - 1) / kRowsPerBlock;
   std::vector<double> part(blocks * L, 0.0);
   std::atomic<size_t> next{0};
   auto work = [&] {
-    std::vector<double> cur(S * L), nxt(S * L);
+    std::vector<double> cur(S * lat.Lc, 0.0), nxt(S * lat.Lc, 0.0);
     for (size_t k; (k = next.fetch_add(1)) < blocks;)
-      exact_counts_rows(J, X, Y, boundary, k * kRowsPerBlock, std::min(rows, (k + 1) * kRowsPerBlock), cur, nxt,
-                        &part[k * L]);
+      exact_counts_rows(lat, k * kRowsPerBlock, std::min(rows, (k + 1) * kRowsPerBlock), cur, nxt, &part[k * L]);
   };
   const size_t threads = std::min<size_t>(blocks, std::max(1u, std::thread::hardware_concurrency()));
   std::vector<std::thread> pool;
   for (size_t t = 1; t < threads; ++t) pool.emplace_back(work);
   work();
   for (std::thread& t : pool) t.join();
-  std::fill(counts, counts + L, 0.0);
   for (size_t k = 0; k < blocks; ++k)
     for (size_t e = 0; e < L; ++e) counts[e] += part[k * L + e];
   for (size_t e = 0; e < L; ++e) counts[e] *= 2.0;

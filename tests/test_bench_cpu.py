@@ -68,3 +68,34 @@ def test_accuracy_scores_exact_curves_as_exact():
     d = acc["class_decisions"]
     assert d["samples"] == 100 and d["engine_equals_exact"] == 99 and d["reference_cuda_equals_exact"] == 0
     assert sum(d["exact_classes"].values()) == 100
+
+
+def test_batched_accuracy_scores_every_side_against_exact():
+    """The batched leg's scoring on curves that are the exact log g of each
+    problem (one periodic and one open per side up to 10, one open 12x12,
+    which the transfer matrix walks in one pass): zero error, energy sets
+    exact, at most the stated number of curves per side, and a problem that
+    did not converge is skipped."""
+    import types
+    import bench
+    import oracle as O
+    probs, out = [], []
+    for L in (4, 6, 8, 10, 12):
+        for boundary in ((0, 1) if L <= 10 else (1,)):
+            p = types.SimpleNamespace(X=L, Y=L, boundary=boundary, sample=3, seed=77, prob=0.08,
+                                      error_class=b"h")
+            N = L * L
+            J = O.init_interactions(L, L, p.sample + 1, p.seed, p.prob, "h")[p.sample * 2 * N:]
+            cnt = O.exact_counts(J, L, L, boundary)
+            E = (np.nonzero(cnt)[0] - 2 * N).astype(np.int32)
+            probs.append(p)
+            out.append((types.SimpleNamespace(status=0), E, np.log(cnt[E + 2 * N])))
+    probs.insert(0, probs[0])
+    out.insert(0, (types.SimpleNamespace(status=3), np.zeros(0, np.int32), np.zeros(0)))
+    acc = bench.batched_accuracy(probs, out)
+    assert set(acc) == {f"{L}x{L}" for L in (4, 6, 8, 10, 12)}
+    for L in (4, 6, 8, 10, 12):
+        a = acc[f"{L}x{L}"]
+        assert a["curves"] == min(2 if L <= 10 else 1, bench.BATCHED_ACCURACY_PER_SIDE[L])
+        assert a["energy_sets_exact"]
+        assert a["rms_mean"] < 1e-12 and a["max_abs"] < 1e-12

@@ -108,6 +108,22 @@ def test_transfer_matrix_10x10_known_answers():
         assert np.allclose(c, c[::-1], rtol=1e-13, atol=0)
 
 
+def test_exact_counts_open_12x12():
+    """The open-boundary transfer matrix (one pass over all first rows) at
+    2^144 states.  Uniform J = +1 on the 264 bonds: 2 ground states at -264;
+    4 corner flips x2 at -260; 40 edge flips and 8 corner-edge pairs x2 at
+    -258; nothing in between.  Random couplings: 2^N states in all and
+    g(E) = g(-E) (the lattice is bipartite)."""
+    L, N = 12, 144
+    c = O.exact_counts(np.ones(2 * N, np.int8), L, L, 1)
+    assert c[-264 + 2 * N] == 2 and c[-260 + 2 * N] == 8 and c[-258 + 2 * N] == 2 * (4 * (L - 2) + 8)
+    assert np.count_nonzero(c[:-264 + 2 * N]) == 0 and c[-262 + 2 * N] == 0 and c[-259 + 2 * N] == 0
+    for cls in "ivhc":
+        c = O.exact_counts(O.init_interactions(L, L, 1, 5, 0.1, cls), L, L, 1)
+        assert abs(c.sum() / 2.0 ** N - 1) < 1e-13
+        assert np.allclose(c, c[::-1], rtol=1e-13, atol=0)
+
+
 def test_error_classes_are_gauge_copies_on_open_lattices_only():
     """The class chains (prerun.cu:56-75) negate a full column of right bonds
     (v) or a full row of down bonds (h).  On an open lattice that is a gauge
