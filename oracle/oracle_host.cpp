@@ -546,13 +546,16 @@ struct ExactLattice {
   int Jr(int i, int j) const { return static_cast<int>(J[i * Y + j]); }
   int Jd(int i, int j) const { return static_cast<int>(J[N + i * Y + j]); }
 
-  // bond terms and energy of a first row
-  int row0_terms() const { return boundary == 0 ? Y : Y - 1; }
+  // bond terms and energy of a first row; a periodic lattice of one row
+  // also holds each spin's down bond to itself (a constant -J)
+  int row0_terms() const { return (boundary == 0 ? Y : Y - 1) + (boundary == 0 && X == 1 ? Y : 0); }
   int row0_energy(size_t r0) const
   {
     int e = 0;
     for (int j = 0; j + 1 < Y; ++j) e -= Jr(0, j) * spin(r0, j) * spin(r0, j + 1);
     if (boundary == 0) e -= Jr(0, Y - 1) * spin(r0, Y - 1) * spin(r0, 0);
+    if (boundary == 0 && X == 1)
+      for (int j = 0; j < Y; ++j) e -= Jd(0, j);
     return e;
   }
 

@@ -80,7 +80,7 @@ def test_flip_ratio():
 @pytest.mark.parametrize("boundary", [0, 1])
 def test_transfer_matrix_equals_enumeration(boundary):
     for seed in (1, 2, 3):
-        for X, Y in ((4, 4), (3, 5), (2, 6), (4, 5), (5, 4), (2, 2)):
+        for X, Y in ((4, 4), (3, 5), (2, 6), (4, 5), (5, 4), (2, 2), (1, 6), (6, 1), (1, 1), (7, 3)):
             J = O.init_interactions(X, Y, 1, seed, 0.3)
             assert np.array_equal(O.exact_counts(J, X, Y, boundary), O.exact_counts(J, X, Y, boundary, brute=True))
 
