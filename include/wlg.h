@@ -283,13 +283,17 @@ wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, w
  * synchronisation, a deployment that forbids allocating after start-up.
  * Every device buffer it needs comes from one fixed 8 MiB arena compiled
  * into the library, which each GPU that loads the library holds until the
- * process exits.  A batch whose worst-case footprint exceeds the arena is
- * rejected with WLG_ERR_CAPACITY before anything runs (400 problems of 6x6
- * lattices fit).  Runs on the current device and `stream`; returns after
- * the stream has finished the batch.  The first call on a device looks up
- * the arena's device address, so make that first call before any stream
- * capture.  All calls share the arena, which keeps the last call's
- * contents: calls that overlap on the GPU race, so serialise them. */
+ * process exits.  A batch whose worst-case footprint (every window as wide
+ * as the full energy range, including the global log g pool of problems too
+ * large for shared memory) exceeds the arena is rejected with
+ * WLG_ERR_CAPACITY before anything runs, leaving results and outputs as the
+ * caller left them (400 problems of 6x6 lattices fit).  Runs on the current
+ * device and `stream`; the call synchronises `stream` itself (after the
+ * pre-run and at the end) and returns once the stream has finished the
+ * batch.  The first call on a device looks up the arena's device address,
+ * so make that first call before any stream capture.  All calls share the
+ * arena, which keeps the last call's contents: calls that overlap on the
+ * GPU race, so serialise them. */
 wlg_status wlg_solve_raw_noalloc(const wlg_problem* problems, int n, wlg_result* results, int* win_start,
                                  int* win_end, double* raw_log_g, long long raw_capacity, long long* raw_offset,
                                  wlg_stream stream);

@@ -1338,16 +1338,35 @@ struct ArenaExec final : Exec {
 
 // Upper bound of the arena bytes a batch needs, from the problem parameters
 // alone (windows of the full range [-2N, 2N], energy step 2), so oversized
-// batches are rejected before anything runs.
+// batches are rejected before anything runs.  This includes the global log g
+// pool of the form-3 launches (run_main): one slice of L x team doubles per
+// resident team, at most (problems + teams per CTA - 1) slices per team size,
+// counted for every problem whose full-range state would not fit shared
+// memory (its real windows are never wider, so no form-3 problem is missed).
 size_t noalloc_bound(const wlg_problem* probs, int n)
 {
   auto pad = [](size_t x) { return (x + 255) & ~size_t{255}; };
   size_t pre_desc = 0, j8 = 0, seen = 0, found = 0, fflag = 0;
   size_t md = 0, order = 0, jw = 0, latw = 0, win = 0, mask = 0, out = 0, res = 0;
+  std::map<int, std::pair<size_t, size_t>> pool;  // team size -> (form-3 problems, largest L)
   for (int p = 0; p < n; ++p) {
     const wlg_problem& q = probs[p];
     const size_t N = static_cast<size_t>(q.X) * q.Y, I = static_cast<size_t>(q.intervals);
     const size_t nwL = (N + 31) / 32, nbins = 2 * N + 1;
+    MainDesc d{};
+    d.X = q.X;
+    d.Y = q.Y;
+    d.N = static_cast<int>(N);
+    d.I = q.intervals;
+    d.L = static_cast<int>(nbins);
+    d.nwL = static_cast<int>(nwL);
+    d.nwM = static_cast<int>((nbins + 31) / 32);
+    const int team = wlg::round32(q.intervals * q.walkers_per_interval);
+    if (wlg::fit_form(d, team) == 3) {
+      auto& e = pool[team];
+      e.first += 1;
+      e.second = std::max(e.second, nbins);
+    }
     pre_desc += sizeof(PreDesc);
     j8 += 2 * N;
     seen += 4 * N + 1;
@@ -1362,8 +1381,13 @@ size_t noalloc_bound(const wlg_problem* probs, int n)
     out += I * nbins * sizeof(double);
     res += sizeof(MainResult);
   }
+  size_t gpool = 0;
+  for (const auto& [team, e] : pool) {
+    const size_t per_cta_max = team <= 256 ? static_cast<size_t>(256 / team) : 1;
+    gpool += (e.first + per_cta_max - 1) * e.second * static_cast<size_t>(team) * sizeof(double);
+  }
   return pad(pre_desc) + pad(j8) + pad(seen) + pad(found) + pad(fflag) + pad(md) + pad(order) + pad(jw) + pad(latw) +
-         pad(win) + pad(mask) + pad(out) + pad(res) + pad(64 * sizeof(int));
+         pad(win) + pad(mask) + pad(out) + pad(res) + pad(64 * sizeof(int)) + pad(gpool);
 }
 
 }  // namespace
