@@ -188,6 +188,25 @@ def reference_harness():
         L.refh_run.argtypes = [i32, i32, i32, f32, C.c_char, i32, i32, i32, i32, i32, i32, i32, f32, f64, f64, i32, i32,
                                i64, P, P, P, P, P, P, i64]
         L.refh_run.restype = C.c_int
+        L.refh_mainrun.argtypes = [i32, i32, i32, i32, i32, i32, P, P, P, P, i32, i32, f32, f64, f64, i32, i32, i64,
+                                   P, P, P, P, P, i64]
+        L.refh_mainrun.restype = C.c_int
+        kernels = {
+            "refh_k_init_interactions": [P, i32, i32, i32, i32, f32, C.c_char],
+            "refh_k_calc_energy": [i32, P, P, P, P, i32, i32, sz, i32],
+            "refh_k_pre_run": [P] * 8 + [i32] * 6 + [u32, i32, sz, i32, i32],
+            "refh_k_init_offsets_histogram": [P] * 4 + [i32] * 3,
+            "refh_k_wang_landau": [P] * 17 + [i32] * 8,
+            "refh_k_check_histogram": [P] * 9 + [f64, i32, i32, i32],
+            "refh_k_average_log_g": [P] * 8 + [i32] * 3,
+            "refh_k_reset_cond": [P, P, i32, f64, i32, i32, i32],
+            "refh_k_check_finished": [P, P, i32, i32],
+            "refh_k_replica_exchange": [P] * 9 + [i32] * 5,
+        }
+        for name, args in kernels.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
         rc = L.refh_open(cubin.encode())
         if rc != 0:
             raise RuntimeError(f"reference cubin could not be loaded (code {rc})")
@@ -278,3 +297,32 @@ def reference_run(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, I, W,
             pos += ln
     return dict(status=st, pre_ms=t_pre.value, main_ms=t_main.value, outer=outer.value, start=starts, end=ends,
                 windows=wins)
+
+
+def reference_mainrun(X, Y, boundary, seed, R, pre_i, seen, couplings, lattices, lattice_energy, I, W, overlap,
+                      alpha, beta, n_iter, xc, max_outer=0):
+    """mainrun.cu alone on the reference's own kernels, from pre-run outputs of
+    samples 0..R-1 (seen [R][4N+1], couplings [R][2N], lattices [R][pre_i][N],
+    zero where none was stored, lattice_energy [R][pre_i]).
+    Returns dict(status, main_ms, outer, start, end, windows)."""
+    L = reference_harness()
+    if L is None:
+        raise RuntimeError("reference cubin not available")
+    t_main, outer = C.c_double(), C.c_longlong()
+    starts = np.zeros(R * I, np.int32)
+    ends = np.zeros(R * I, np.int32)
+    cap = R * I * (4 * X * Y + 1)
+    raw = np.zeros(cap, np.float64)
+    a = [np.ascontiguousarray(seen, np.uint8), np.ascontiguousarray(couplings, np.int8),
+         np.ascontiguousarray(lattices, np.int8), np.ascontiguousarray(lattice_energy, np.int32)]
+    st = L.refh_mainrun(X, Y, boundary, seed, R, pre_i, ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(a[3]), I, W,
+                        C.c_float(overlap), alpha, beta, n_iter, xc, max_outer, C.byref(t_main), C.byref(outer),
+                        ptr(starts), ptr(ends), ptr(raw), cap)
+    wins = []
+    if st in (0, 3):
+        pos = 0
+        for q in range(R * I):
+            ln = int(ends[q] - starts[q] + 1)
+            wins.append(raw[pos:pos + ln].copy())
+            pos += ln
+    return dict(status=st, main_ms=t_main.value, outer=outer.value, start=starts, end=ends, windows=wins)

@@ -21,7 +21,8 @@ OUT = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(OUT, "wl_ref.cubin")
 HARNESS = os.path.join(OUT, "libref_harness.so")
 HOST = os.path.join(OUT, "libref_host.so")
-REFERENCE = "/root/reference"
+# where the reference project's sources lie (only read when present)
+REFERENCE = os.environ.get("WLG_REFERENCE_DIR", "/root/reference")
 
 
 def build_cubin() -> str | None:

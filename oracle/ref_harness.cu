@@ -174,23 +174,27 @@ int refh_open(const char* cubin)
   return 0;
 }
 
-// prerun.cu then mainrun.cu for R samples of one error class, exactly as
-// the reference runs them (its exchange counter never advances, so
-// replica exchange runs only when xc == 1).  Outputs: pre-run and main-run
-// wall time (ms, device-synchronised), outer iterations, a status (0
-// converged, 1 new energy, 2 hand-off error, 3 iteration cap, >= 10 launch
-// error) and, when raw != nullptr, walker 0's dense log g of every window
-// (sample after sample) with the window bounds.
-int refh_run(int X, int Y, int boundary, float prob, char cls, int seed, int R, int pre_w, int pre_i, int pre_n, int I,
-             int W, float overlap, double alpha, double beta, int n_iter, int xc, long long max_outer, double* t_pre,
-             double* t_main, long long* outer_out, int* starts, int* ends, double* raw, long long raw_cap)
+}  // extern "C"
+
+namespace {
+
+// Host copies of what prerun.cu writes to prerun_results.h5 for R samples
+// (file_io.cpp:23-192): the binary histogram [R][4N+1], the couplings
+// [R][2N], the stored lattices [R][pre_i][N] (all zero where none was
+// stored) and their energies.
+struct PreOut {
+  std::vector<unsigned long long> hist;
+  std::vector<int8_t> J, found;
+  std::vector<int> energy;
+};
+
+// prerun.cu:23-146 on the reference's kernels.
+int run_prerun(int X, int Y, int boundary, float prob, char cls, int seed, int R, int pre_w, int pre_i, int pre_n,
+               PreOut& po)
 {
-  if (g_mod == nullptr) return 20;
   const int N = X * Y;
   unsigned int bnd = static_cast<unsigned>(boundary);
   Dev dv;
-  auto t0 = std::chrono::steady_clock::now();
-  // ------------------------------------------------ prerun.cu:23-146
   const int e_min = -2 * N, e_max = -e_min;
   std::vector<int> ps, pe;
   long long ptot = 0;
@@ -232,18 +236,37 @@ int refh_run(int X, int Y, int boundary, float prob, char cls, int seed, int R, 
                 &pre_w, &bnd});
   rc |= launch(energy_fn, B_INT, T, {&d_ienergy, &d_found, &d_J, &d_off_i, &X, &Y, &ni, &pre_i});
   if (rc != 0) return 10;
-  std::vector<int> h_ienergy(total_intervals);
-  std::vector<int8_t> h_J(static_cast<size_t>(R) * N * 2), h_found(static_cast<size_t>(total_intervals) * N);
-  std::vector<unsigned long long> h_hist(total_histogram);
-  cudaMemcpy(h_ienergy.data(), d_ienergy, h_ienergy.size() * 4, cudaMemcpyDeviceToHost);
-  cudaMemcpy(h_J.data(), d_J, h_J.size(), cudaMemcpyDeviceToHost);
-  cudaMemcpy(h_found.data(), d_found, h_found.size(), cudaMemcpyDeviceToHost);
-  cudaMemcpy(h_hist.data(), d_histogram, h_hist.size() * 8, cudaMemcpyDeviceToHost);
+  po.energy.assign(total_intervals, 0);
+  po.J.assign(static_cast<size_t>(R) * N * 2, 0);
+  po.found.assign(static_cast<size_t>(total_intervals) * N, 0);
+  po.hist.assign(total_histogram, 0);
+  cudaMemcpy(po.energy.data(), d_ienergy, po.energy.size() * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(po.J.data(), d_J, po.J.size(), cudaMemcpyDeviceToHost);
+  cudaMemcpy(po.found.data(), d_found, po.found.size(), cudaMemcpyDeviceToHost);
+  cudaMemcpy(po.hist.data(), d_histogram, po.hist.size() * 8, cudaMemcpyDeviceToHost);
   if (cudaDeviceSynchronize() != cudaSuccess) return 12;
-  *t_pre = ms_since(t0);
+  return 0;
+}
 
+// The hand-off (file_io.cpp:558-659) and mainrun.cu:42-383 on the
+// reference's kernels, from pre-run outputs.  Outputs as refh_run.
+int run_mainrun(int X, int Y, int boundary, int seed, int R, int pre_i, const PreOut& po, int I, int W, float overlap,
+                double alpha, double beta, int n_iter, int xc, long long max_outer, double* t_main,
+                long long* outer_out, int* starts, int* ends, double* raw, long long raw_cap)
+{
+  const int N = X * Y;
+  unsigned int bnd = static_cast<unsigned>(boundary);
+  Dev dv;
+  const int e_min = -2 * N;
+  const unsigned len_histogram = static_cast<unsigned>(4 * N + 1);
+  const char* energy_fn = boundary == 1 ? "wl::calc_energy_open_boundary(" : "wl::calc_energy_periodic_boundary(";
+  const std::vector<unsigned long long>& h_hist = po.hist;
+  const std::vector<int8_t>& h_J = po.J;
+  const std::vector<int8_t>& h_found = po.found;
+  const std::vector<int>& h_ienergy = po.energy;
+  int rc = 0;
+  auto t0 = std::chrono::steady_clock::now();
   // ------------------------------------------------ mainrun.cu:42-228
-  t0 = std::chrono::steady_clock::now();
   const int total_walker_m = R * I * W, total_intervals_m = R * I, wpi = I * W;
   std::vector<int8_t> spectrum;
   std::vector<int> off_spec, h_start, h_end, len_hist_k;
@@ -302,7 +325,9 @@ int refh_run(int X, int Y, int boundary, float prob, char cls, int seed, int R, 
   auto* dm_logG = dv.zeros<double>(static_cast<size_t>(total_len));
   auto* dm_shared = dv.zeros<double>(static_cast<size_t>(size_shared));
   auto* dm_off_shared = dv.from(off_shared);
-  auto* dm_off_hist = dv.zeros<int>(static_cast<size_t>(total_walker_m));
+  // one entry more than walkers: calc_average_log_g and redistribute_g_values
+  // read d_offset_histogram[R*I*W] while looking up the last sample (wl.cu:737, :1001)
+  auto* dm_off_hist = dv.zeros<int>(static_cast<size_t>(total_walker_m) + 1);
   auto* dm_off_lat = dv.zeros<int>(static_cast<size_t>(total_walker_m));
   auto* dm_off_iter = dv.zeros<unsigned long>(static_cast<size_t>(total_walker_m));
   auto* dm_factor = dv.from(std::vector<double>(static_cast<size_t>(total_walker_m), std::numbers::e));
@@ -407,6 +432,206 @@ int refh_run(int X, int Y, int boundary, float prob, char cls, int seed, int R, 
     }
   }
   return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+// prerun.cu then mainrun.cu for R samples of one error class, exactly as
+// the reference runs them (its exchange counter never advances, so
+// replica exchange runs only when xc == 1).  Outputs: pre-run and main-run
+// wall time (ms, device-synchronised), outer iterations, a status (0
+// converged, 1 new energy, 2 hand-off error, 3 iteration cap, >= 10 launch
+// error) and, when raw != nullptr, walker 0's dense log g of every window
+// (sample after sample) with the window bounds.
+int refh_run(int X, int Y, int boundary, float prob, char cls, int seed, int R, int pre_w, int pre_i, int pre_n, int I,
+             int W, float overlap, double alpha, double beta, int n_iter, int xc, long long max_outer, double* t_pre,
+             double* t_main, long long* outer_out, int* starts, int* ends, double* raw, long long raw_cap)
+{
+  if (g_mod == nullptr) return 20;
+  PreOut po;
+  const auto t0 = std::chrono::steady_clock::now();
+  const int rc = run_prerun(X, Y, boundary, prob, cls, seed, R, pre_w, pre_i, pre_n, po);
+  if (rc != 0) return rc;
+  *t_pre = ms_since(t0);
+  return run_mainrun(X, Y, boundary, seed, R, pre_i, po, I, W, overlap, alpha, beta, n_iter, xc, max_outer, t_main,
+                     outer_out, starts, ends, raw, raw_cap);
+}
+
+// mainrun.cu alone, on the reference's kernels, from given pre-run outputs
+// of R samples (samples 0..R-1 of a run seeded `seed`) in the layout the
+// reference writes to prerun_results.h5: seen [R][4N+1] (nonzero where the
+// pre-run visited energy -2N + i), couplings [R][2N], stored lattices
+// [R][pre_i][N] (all zero where none was stored) and their energies
+// [R][pre_i].  Outputs as refh_run.
+int refh_mainrun(int X, int Y, int boundary, int seed, int R, int pre_i, const unsigned char* seen,
+                 const int8_t* couplings, const int8_t* lattices, const int* lattice_energy, int I, int W,
+                 float overlap, double alpha, double beta, int n_iter, int xc, long long max_outer, double* t_main,
+                 long long* outer_out, int* starts, int* ends, double* raw, long long raw_cap)
+{
+  if (g_mod == nullptr) return 20;
+  const size_t N = static_cast<size_t>(X) * Y;
+  PreOut po;
+  po.hist.assign(seen, seen + R * (4 * N + 1));
+  po.J.assign(couplings, couplings + R * 2 * N);
+  po.found.assign(lattices, lattices + static_cast<size_t>(R) * pre_i * N);
+  po.energy.assign(lattice_energy, lattice_energy + static_cast<size_t>(R) * pre_i);
+  return run_mainrun(X, Y, boundary, seed, R, pre_i, po, I, W, overlap, alpha, beta, n_iter, xc, max_outer, t_main,
+                     outer_out, starts, ends, raw, raw_cap);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// One reference kernel at a time on caller-owned device state in the
+// reference's layout, launched with the geometry of its drivers.  Every
+// pointer is a device address; each call synchronises the device and returns
+// 0, 10/11 on a missing kernel or failed launch, 12 on a device error.
+
+namespace {
+
+int finish(int rc)
+{
+  if (rc != 0) return rc;
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 12;
+}
+
+unsigned blocks128(size_t n) { return static_cast<unsigned>((n + 127) / 128); }
+
+}  // namespace
+
+extern "C" {
+
+// wl::init_interactions then the class's chains, prerun.cu:52-75.
+int refh_k_init_interactions(void* J, int X, int Y, int R, int seed, float prob, char cls)
+{
+  size_t lsz = static_cast<size_t>(X) * Y;
+  const unsigned g = blocks128(lsz * 2 * R);
+  int rc = launch("wl::init_interactions(", g, 128, {&J, &lsz, &R, &seed, &prob});
+  if (cls == 'h' || cls == 'c') rc |= launch("wl::apply_x_horizontal_error(", g, 128, {&J, &X, &Y, &R});
+  if (cls == 'v' || cls == 'c') rc |= launch("wl::apply_x_vertical_error(", g, 128, {&J, &X, &Y, &R});
+  return finish(rc);
+}
+
+// wl::calc_energy_periodic_boundary / wl::calc_energy_open_boundary (wl.cu:261-340).
+int refh_k_calc_energy(int boundary, void* energy, void* lattice, void* J, void* off_lat, int X, int Y,
+                       size_t num_lattices, int wpi)
+{
+  const char* fn = boundary == 1 ? "wl::calc_energy_open_boundary(" : "wl::calc_energy_periodic_boundary(";
+  return finish(launch(fn, blocks128(num_lattices), 128, {&energy, &lattice, &J, &off_lat, &X, &Y, &num_lattices, &wpi}));
+}
+
+// wl::wang_landau_pre_run (wl.cu:473-560), prerun.cu:103 geometry.
+int refh_k_pre_run(void* energy, void* flag_found, void* lattice, void* found_lattice, void* histogram,
+                   void* seed_offset, void* J, void* off_lat, int e_min, int e_max, int n_iter, int X, int Y, int seed,
+                   unsigned num_intervals, int len_interval, size_t num_walkers, int wpi, int boundary)
+{
+  unsigned bnd = static_cast<unsigned>(boundary);
+  return finish(launch("wl::wang_landau_pre_run(", blocks128(num_walkers), 128,
+                       {&energy, &flag_found, &lattice, &found_lattice, &histogram, &seed_offset, &J, &off_lat, &e_min,
+                        &e_max, &n_iter, &X, &Y, &seed, &num_intervals, &len_interval, &num_walkers, &wpi, &bnd}));
+}
+
+// wl::init_offsets_histogram (wl.cu:615-652), mainrun.cu:177 geometry:
+// grid = windows, block = walkers per window.
+int refh_k_init_offsets_histogram(void* off_hist, void* start, void* end, void* len_hist, int I, int W,
+                                  int total_walkers)
+{
+  return finish(launch("wl::init_offsets_histogram(", static_cast<unsigned>(total_walkers / W),
+                       static_cast<unsigned>(W), {&off_hist, &start, &end, &len_hist, &I, &total_walkers}));
+}
+
+// wl::wang_landau (wl.cu:1033-1175), mainrun.cu:245 geometry.
+int refh_k_wang_landau(void* lattice, void* J, void* H, void* logG, void* factor, void* energy, void* new_energy,
+                       void* offset_iter, void* found, void* start, void* end, void* off_hist, void* off_lat, void* cond,
+                       void* spectrum, void* off_spec, void* cond_inter, int X, int Y, int n_iter, int num_lattices,
+                       int I, int wpi, int seed, int boundary)
+{
+  unsigned bnd = static_cast<unsigned>(boundary);
+  const int W = wpi / I;
+  return finish(launch("wl::wang_landau(", static_cast<unsigned>(num_lattices / W), static_cast<unsigned>(W),
+                       {&lattice, &J, &H, &logG, &factor, &energy, &new_energy, &offset_iter, &found, &start, &end,
+                        &off_hist, &off_lat, &cond, &spectrum, &off_spec, &cond_inter, &X, &Y, &n_iter, &num_lattices,
+                        &I, &wpi, &seed, &bnd}));
+}
+
+// wl::check_histogram (wl.cu:892-967), mainrun.cu:285 geometry.
+int refh_k_check_histogram(void* H, void* factor, void* cond, void* off_hist, void* end, void* start, void* spectrum,
+                           void* off_spec, void* cond_inter, double alpha, int num_walkers, int wpi, int I)
+{
+  const int W = wpi / I;
+  return finish(launch("wl::check_histogram(", static_cast<unsigned>(num_walkers / W), static_cast<unsigned>(W),
+                       {&H, &factor, &cond, &off_hist, &end, &start, &spectrum, &off_spec, &cond_inter, &alpha,
+                        &num_walkers, &wpi, &I}));
+}
+
+// wl::calc_average_log_g then wl::redistribute_g_values (wl.cu:710-783,
+// :969-1031), mainrun.cu:299-329: the scratch arrays the reference's driver
+// keeps (per-sample histogram lengths, per-window offsets into the shared
+// log g buffer, the zeroed buffer itself) are built here from start/end.
+int refh_k_average_log_g(void* logG, void* start, void* end, void* spectrum, void* cond, void* off_hist,
+                         void* off_spec, void* cond_inter, int R, int W, int I)
+{
+  const int nwin = R * I;
+  std::vector<int> h_start(static_cast<size_t>(nwin)), h_end(static_cast<size_t>(nwin));
+  cudaMemcpy(h_start.data(), start, h_start.size() * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(h_end.data(), end, h_end.size() * 4, cudaMemcpyDeviceToHost);
+  std::vector<int> len_hist(static_cast<size_t>(R), 0);
+  std::vector<long long> off_shared(static_cast<size_t>(nwin));
+  long long size_shared = 0, total = 0;
+  for (int q = 0; q < nwin; ++q) {
+    const int len = h_end[q] - h_start[q] + 1;
+    off_shared[q] = size_shared;
+    size_shared += len;
+    len_hist[q / I] += W * len;
+    total += static_cast<long long>(W) * len;
+  }
+  Dev dv;
+  auto* d_len = dv.from(len_hist);
+  auto* d_off_shared = dv.from(off_shared);
+  auto* d_shared = dv.zeros<double>(static_cast<size_t>(size_shared));
+  // the walker offsets plus one entry: both kernels read index R*I*W (wl.cu:737, :1001)
+  auto* d_off_hist = dv.zeros<int>(static_cast<size_t>(nwin) * W + 1);
+  cudaMemcpy(d_off_hist, off_hist, static_cast<size_t>(nwin) * W * 4, cudaMemcpyDeviceToDevice);
+  int tlh = static_cast<int>(total);
+  const unsigned g = blocks128(static_cast<size_t>(total));
+  int rc = launch("wl::calc_average_log_g(", g, 128,
+                  {&d_shared, &d_len, &logG, &start, &end, &spectrum, &cond, &d_off_hist, &off_spec, &d_off_shared,
+                   &cond_inter, &R, &W, &I, &tlh});
+  rc |= launch("wl::redistribute_g_values(", g, 128,
+               {&logG, &d_shared, &d_len, &start, &end, &cond_inter, &d_off_hist, &cond, &d_off_shared, &I, &W, &R,
+                &tlh});
+  return finish(rc);
+}
+
+// wl::reset_d_cond (wl.cu:596-613), mainrun.cu:331 geometry.
+int refh_k_reset_cond(void* cond, void* factor, int total_intervals, double beta, int W, int R, int I)
+{
+  return finish(launch("wl::reset_d_cond(", static_cast<unsigned>(R), static_cast<unsigned>(I),
+                       {&cond, &factor, &total_intervals, &beta, &W}));
+}
+
+// wl::check_interactions_finished (wl.cu:662-708): the segmented sum of cond
+// per sample, then the reference's check_all_intervals_finished kernel.
+int refh_k_check_finished(void* cond_inter, void* cond, int I, int R)
+{
+  h_segsum<<<(R + 127) / 128, 128>>>(static_cast<const int8_t*>(cond), I, R, static_cast<int*>(cond_inter));
+  if (cudaDeviceSynchronize() != cudaSuccess) return 12;
+  return finish(launch("check_all_intervals_finished(", static_cast<unsigned>(R), 1, {&cond_inter, &I, &R}));
+}
+
+// wl::replica_exchange with its Fisher-Yates shuffle (wl.cu:785-890), one
+// parity, mainrun.cu:347-371 geometry.
+int refh_k_replica_exchange(void* off_lat, void* energy, void* indices, void* offset_iter, void* start, void* end,
+                            void* off_hist, void* cond_inter, void* logG, int even, int seed, int I, int wpi,
+                            int total_intervals)
+{
+  bool ev = even != 0;
+  const int W = wpi / I;
+  return finish(launch("wl::replica_exchange(", static_cast<unsigned>(total_intervals), static_cast<unsigned>(W),
+                       {&off_lat, &energy, &indices, &offset_iter, &start, &end, &off_hist, &cond_inter, &logG, &ev,
+                        &seed, &I, &wpi}));
 }
 
 }  // extern "C"
