@@ -45,7 +45,18 @@ METRIC = "disorder samples converged/s (6x6 periodic p=0.04, 100 samples x 4 cla
 CPU_SAMPLE_PROBLEMS = 96
 
 
-def problems(rank: int = 0):
+def r4(x):
+    """Floats to four significant digits, recursively (keeps the line short)."""
+    if isinstance(x, float):
+        return float(f"{x:.4g}") if np.isfinite(x) else None
+    if isinstance(x, dict):
+        return {k: r4(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [r4(v) for v in x]
+    return x
+
+
+def problems(rank: int = 0, exchange_mode: int = 1):
     import qec_pf_wang_landau_gb300 as wlg
     w = WORKLOAD
     out = []
@@ -56,7 +67,8 @@ def problems(rank: int = 0):
                                    pre_intervals=w["pre_intervals"], pre_iterations=w["pre_iterations"],
                                    intervals=w["intervals"], walkers_per_interval=w["walkers_per_interval"],
                                    overlap=w["overlap"], alpha=w["alpha"], beta=w["beta"],
-                                   iterations=w["iterations"], exchange_every=w["exchange_every"], exchange_mode=1))
+                                   iterations=w["iterations"], exchange_every=w["exchange_every"],
+                                   exchange_mode=exchange_mode))
     return out
 
 
@@ -116,6 +128,23 @@ def reference_cuda_run():
     return conv / (tot_ms / 1e3), tot_ms / 1e3, runs
 
 
+def engine_x0_run(ctx, steps: int):
+    """This engine on the same 400 problems with the reference's exchange
+    behaviour at -c 20 (its counter never advances: no exchange), timed like
+    the headline (pre-run + hand-off + main-run device time): the arm that
+    runs the same algorithm as the reference's kernels.  Returns
+    (converged samples/s, outputs of the last solve)."""
+    probs = problems(0, exchange_mode=0)
+    ctx.solve(probs)
+    t, conv, out = 0.0, 0, None
+    for _ in range(steps):
+        out = ctx.solve(probs)
+        st = ctx.stats()
+        t += (st["pre_ms"] + st["handoff_ms"] + st["main_ms"]) / 1e3
+        conv += sum(1 for r, _, _ in out if r.status == 0)
+    return conv / t, out
+
+
 ACCURACY_SAMPLES = 8
 
 
@@ -137,60 +166,53 @@ def _reference_curve(run, k, X, Y, I):
     return (Er[:n.value], Gr[:n.value]) if rc == 0 else None
 
 
-def accuracy(out, ref_runs):
+def accuracy(arms, ref_runs):
     """log g error after normalisation against the exact density of states
     (transfer matrix over all 2^36 states) for samples 0-7 of every class:
-    RMS and max |log g - log g_exact| per curve, this engine's (from the timed
-    run's own output) and the reference kernels'.  And the logical-class
-    decision of every sample (argmax over classes of log Z_c =
-    logsumexp(log g_c(E) - beta_N E) at the Nishimori temperature), compared
-    between the engine, the reference's kernels and the exact counts."""
+    mean RMS and max |log g - log g_exact| over those curves, for every
+    engine arm (from its timed run's own output) and for the reference's
+    kernels.  And the logical-class decision of every sample (argmax over
+    classes of log Z_c = logsumexp(log g_c(E) - beta_N E) at the Nishimori
+    temperature) compared with the exact counts' decision.
+    arms: {name: wlg_solve outputs of the 400 problems}."""
     import oracle as O
     w = WORKLOAD
     X, Y, N, I = w["X"], w["Y"], w["X"] * w["Y"], w["intervals"]
     classes = w["classes"]
     bn = 0.5 * np.log((1.0 - w["prob"]) / w["prob"])
-    res = {"engine": [], "reference_cuda": []}
+    names = list(arms) + ["reference_cuda"]
+    errs = {k: [] for k in names}
     same_sets = True
     Js = {c: O.init_interactions(X, Y, w["samples"], w["seed"], w["prob"], c) for c in classes}
-    decisions = {"engine": [], "reference_cuda": [], "exact": []}
+    decisions = {k: [] for k in names + ["exact"]}
     for k in range(w["samples"]):
         lz = {key: [] for key in decisions}
         for ci, c in enumerate(classes):
             cnt = O.exact_counts(Js[c][k * 2 * N:(k + 1) * 2 * N], X, Y, w["boundary"])
             Ee = np.nonzero(cnt)[0] - 2 * N
             lz["exact"].append(np.logaddexp.reduce(np.log(cnt[Ee + 2 * N]) - bn * Ee))
-            r, E, G = out[k * len(classes) + ci]
-            lz["engine"].append(np.logaddexp.reduce(G - bn * E) if r.status == 0 else np.nan)
-            ref = _reference_curve(None if ref_runs is None else ref_runs.get(c), k, X, Y, I)
-            lz["reference_cuda"].append(np.logaddexp.reduce(ref[1] - bn * ref[0]) if ref is not None else np.nan)
-            if k >= ACCURACY_SAMPLES:
-                continue
-            if r.status == 0:
-                same_sets &= set(E.tolist()) == set(Ee.tolist())
-                err = G - np.log(cnt[E + 2 * N])
-                res["engine"].append((float(np.sqrt(np.mean(err ** 2))), float(np.abs(err).max())))
-            if ref is not None:
-                e = ref[1] - np.log(cnt[ref[0] + 2 * N])
-                res["reference_cuda"].append((float(np.sqrt(np.mean(e ** 2))), float(np.abs(e).max())))
+            curves = {}
+            for name, out in arms.items():
+                r, E, G = out[k * len(classes) + ci]
+                curves[name] = (E, G) if r.status == 0 else None
+            curves["reference_cuda"] = _reference_curve(None if ref_runs is None else ref_runs.get(c), k, X, Y, I)
+            for name, cv in curves.items():
+                lz[name].append(np.logaddexp.reduce(cv[1] - bn * cv[0]) if cv is not None else np.nan)
+                if k < ACCURACY_SAMPLES and cv is not None:
+                    if name != "reference_cuda":
+                        same_sets &= set(cv[0].tolist()) == set(Ee.tolist())
+                    err = cv[1] - np.log(cnt[cv[0] + 2 * N])
+                    errs[name].append((float(np.sqrt(np.mean(err ** 2))), float(np.abs(err).max())))
         for key, v in lz.items():
             decisions[key].append(int(np.argmax(v)) if np.all(np.isfinite(v)) else -1)
-    summary = {"curves": f"samples 0-{ACCURACY_SAMPLES - 1} x classes {classes}",
-               "exact": "transfer-matrix density of states over all 2^36 states",
-               "engine_energy_sets_exact": bool(same_sets)}
-    for key, v in res.items():
-        if v:
-            summary[key] = {"rms_mean": float(np.mean([a for a, _ in v])), "max_abs": float(max(b for _, b in v)),
-                            "curves": len(v)}
     d = {key: np.array(v) for key, v in decisions.items()}
-    summary["class_decisions"] = {
-        "samples": w["samples"],
-        "engine_equals_exact": int(np.sum((d["engine"] == d["exact"]) & (d["engine"] >= 0))),
-        "engine_equals_reference_cuda": int(np.sum((d["engine"] == d["reference_cuda"]) & (d["engine"] >= 0))),
-        "reference_cuda_equals_exact": int(np.sum((d["reference_cuda"] == d["exact"]) & (d["reference_cuda"] >= 0))),
-        "exact_classes": {c: int(np.sum(d["exact"] == ci)) for ci, c in enumerate(classes)},
-    }
-    return summary
+    return {"exact": "transfer matrix, 2^36 states", "curves": f"samples 0-{ACCURACY_SAMPLES - 1} x {classes}",
+            "rms": {k: float(np.mean([a for a, _ in v])) for k, v in errs.items() if v},
+            "max": {k: float(max(b for _, b in v)) for k, v in errs.items() if v},
+            "engine_sets_exact": bool(same_sets),
+            "class_decisions_equal_exact": {k: int(np.sum((d[k] == d["exact"]) & (d[k] >= 0))) for k in names},
+            "samples": w["samples"],
+            "exact_class_counts": {c: int(np.sum(d["exact"] == ci)) for ci, c in enumerate(classes)}}
 
 
 SERVING = dict(rate=200.0, seconds=1.0, side_min=4, side_max=16, prob_min=0.02, prob_max=0.12, beta=1e-6,
@@ -201,7 +223,7 @@ def serving_requests(n_max: int = 100000):
     """Poisson arrival times and decoding requests of the serving workload:
     square periodic lattices with side uniform in {4..16}, p uniform in
     [0.02, 0.12], ln f 1e-6, windows scaled with N (N/16, 4..16), 4 walkers
-    each, pre-run 128 walkers x 100 N iterations; all four classes per
+    each, pre-run 128 walkers x 400 N iterations; all four classes per
     request (the server runs them)."""
     import qec_pf_wang_landau_gb300 as wlg
     c = SERVING
@@ -215,7 +237,7 @@ def serving_requests(n_max: int = 100000):
         N = L * L
         arrivals.append(t)
         reqs.append(wlg.problem(L, L, prob=float(rng.uniform(c["prob_min"], c["prob_max"])), seed=c["seed"],
-                                sample=len(reqs), pre_walkers=128, pre_intervals=32, pre_iterations=100 * N,
+                                sample=len(reqs), pre_walkers=128, pre_intervals=32, pre_iterations=400 * N,
                                 intervals=int(min(16, max(4, N // 16))), walkers_per_interval=c["walkers_per_interval"],
                                 overlap=0.25, alpha=0.8, beta=c["beta"], iterations=1000, exchange_every=10))
     return arrivals, reqs
@@ -251,7 +273,8 @@ def serving_run():
             "requests": len(ids), "retired": len(done), "retired_ok": statuses.get("0", 0), "status_counts": statuses,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "throughput_req_s": len(done) / span_s if done else 0.0,
-            "epochs": st["epochs"], "prerun_launches": st["prerun_launches"],
+            "epochs": st["epochs"], "prerun_launches": st["prerun_launches"], "readmitted": st["readmitted"],
+            "requests_readmitted": sum(1 for d in done if d.readmissions > 0),
             "note": f"requests not retired within {SERVING['wait_s']:.0f} s are left out of the percentiles"}
 
 
@@ -298,7 +321,40 @@ def batched_run():
             "value": counts.get("0", 0) / dev_s, "unit": "samples/s", "e2e_samples_per_s": counts.get("0", 0) / wall,
             "status_counts": counts, "flips_per_s": flips / (st["main_ms"] / 1e3), "pre_ms": st["pre_ms"],
             "main_ms": st["main_ms"], "main_forms": st["main_forms"], "kernel_launches": st["kernel_launches"],
-            "accuracy": batched_accuracy(probs, out)}
+            **critical_path(ctx, probs, out), "accuracy": batched_accuracy(probs, out)}
+
+
+def critical_path(ctx, probs, out):
+    """Where a batch's main-run time goes, from each problem's start and end
+    on the device clock: the longest single problem (its own serial chain of
+    outer iterations; no schedule can finish the batch sooner), when problems
+    finish, and how busy the teams were (sum of problem spans / (main-run
+    time x most problems running at once))."""
+    t0, t1 = ctx.main_times()
+    ran = t0 >= 0
+    if not np.any(ran):
+        return {}
+    span = np.where(ran, t1 - t0, 0.0)
+    q = int(np.argmax(span))
+    r = out[q][0]
+    ev = sorted([(a, 1) for a in t0[ran]] + [(b, -1) for b in t1[ran]])
+    live = peak = 0
+    for _, d in ev:
+        live += d
+        peak = max(peak, live)
+    by_side = {}
+    for p, sp, ok in zip(probs, span, ran):
+        if ok:
+            by_side.setdefault(f"{p.X}x{p.Y}", []).append(sp)
+    return {"critical_path_ms": float(span[q]),
+            "critical_problem": {"side": probs[q].X, "boundary": probs[q].boundary, "windows": probs[q].intervals,
+                                 "outer_iterations": int(r.outer_iterations),
+                                 "us_per_outer": 1e3 * float(span[q]) / max(int(r.outer_iterations), 1)},
+            "last_end_ms": float(t1[ran].max()),
+            "end_ms_p50_p90": [float(np.percentile(t1[ran], 50)), float(np.percentile(t1[ran], 90))],
+            "span_ms_max_by_side": {k: float(max(v)) for k, v in sorted(by_side.items())},
+            "concurrent_peak": peak,
+            "team_busy_frac": float(span.sum() / (peak * t1[ran].max()))}
 
 
 # curves scored per side: a periodic 12x12 curve takes tens of seconds of
@@ -327,6 +383,199 @@ def batched_accuracy(probs, out):
         if errs:
             res[f"{L}x{L}"] = {"curves": len(errs), "rms_mean": float(np.mean([a for a, _ in errs])),
                                "max_abs": float(max(b for _, b in errs)), "energy_sets_exact": bool(same)}
+    return res
+
+
+C3_ARMS = dict(seed=7000, sides=(4, 6, 8, 10, 12), per_group=3, beta=1e-6)
+
+
+def c3_group_problems(exchange_mode: int, per_group: int, sides=None):
+    """A subset of the heterogeneous workload laid out as the reference's
+    programs would run it: one group per (side, boundary, class), each group a
+    run of samples 0..R-1 with its own bond probability (uniform in
+    [0.02, 0.12]) and seed; windows N/8 in [8, 32], 4 walkers, overlap 0.25,
+    flatness 0.8, ln f 1e-6, exchange every 10 iterations."""
+    import qec_pf_wang_landau_gb300 as wlg
+    c = C3_ARMS
+    rng = np.random.default_rng(c["seed"])
+    out, g = [], 0
+    for L in (sides or c["sides"]):
+        for b in (0, 1):
+            for cls in "ivhc":
+                prob = float(np.float32(rng.uniform(0.02, 0.12)))
+                N = L * L
+                for k in range(per_group):
+                    out.append(wlg.problem(L, L, boundary=b, prob=prob, error_class=cls, seed=c["seed"] + 100 * g,
+                                           sample=k, pre_walkers=128, pre_intervals=32, pre_iterations=100 * N,
+                                           intervals=int(min(32, max(8, N // 8))), walkers_per_interval=4,
+                                           overlap=0.25, alpha=0.8, beta=c["beta"], iterations=1000,
+                                           exchange_every=10, exchange_mode=exchange_mode))
+                g += 1
+    return out
+
+
+def _groups(probs):
+    """Runs of the reference's programs: consecutive problems that share all but the sample."""
+    runs = []
+    for q, p in enumerate(probs):
+        if p.sample == 0:
+            runs.append([q])
+        else:
+            runs[-1].append(q)
+    return runs
+
+
+def _exact_rms(p, E, G):
+    import oracle as O
+    N = p.X * p.Y
+    J = O.init_interactions(p.X, p.Y, p.sample + 1, p.seed, p.prob, p.error_class.decode())[p.sample * 2 * N:]
+    cnt = O.exact_counts(J, p.X, p.Y, p.boundary)
+    err = G - np.log(cnt[E + 2 * N])
+    return float(np.sqrt(np.mean(err ** 2))), set(E.tolist()) == set((np.nonzero(cnt)[0] - 2 * N).tolist())
+
+
+def c3_arms_run(per_group=None, sides=None, ref_budget_s=600.0):
+    """The heterogeneous workload's comparison (grouped subset, c3_group_problems):
+    this engine batched (every group in one wlg_solve; exchange every 10, and
+    with the reference's exchange behaviour, mode 0), the plain form (the
+    reference's structure on this engine's operators, one run per group) and
+    the reference's own kernels (one prerun + mainrun per group, as its
+    programs run; no exchange, its counter never advances).  Converged
+    samples/s of each, and the log g RMS against exact counts of each arm on
+    the same curves (sample 0 of every group up to 10x10, open 12x12)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    import oracle as O
+    R = per_group or C3_ARMS["per_group"]
+    probs = {m: c3_group_problems(m, R, sides) for m in (0, 1)}
+    ctx = wlg.Context(0)
+    res, outs = {}, {}
+    for m, name in ((1, "engine"), (0, "engine_x0")):
+        ctx.solve(probs[m][:8])  # warm the context's buffers
+        t0 = time.perf_counter()
+        out = ctx.solve(probs[m])
+        wall = time.perf_counter() - t0
+        st = ctx.stats()
+        ok = sum(1 for r, _, _ in out if r.status == 0)
+        res[name] = {"value": ok / ((st["pre_ms"] + st["handoff_ms"] + st["main_ms"]) / 1e3), "wall_s": wall,
+                     "e2e": ok / wall, "converged": ok, **{k: v for k, v in critical_path(ctx, probs[m], out).items()
+                                                           if k in ("critical_path_ms", "last_end_ms")}}
+        outs[name] = out
+    t0 = time.perf_counter()
+    out_p, launches = wlg.solve_plain(probs[0])
+    wall = time.perf_counter() - t0
+    ok = sum(1 for r, _, _ in out_p if r.status == 0)
+    res["plain"] = {"value": ok / wall, "wall_s": wall, "converged": ok, "kernel_launches": launches}
+    outs["plain"] = out_p
+    if O.reference_harness() is not None:
+        ref_out = [None] * len(probs[0])
+        tot_ms, ok, done_groups = 0.0, 0, 0
+        runs = _groups(probs[0])
+        for run in runs:
+            if tot_ms / 1e3 > ref_budget_s:
+                break
+            p = probs[0][run[0]]
+            o = O.reference_run(p.X, p.Y, p.boundary, p.prob, p.error_class.decode(), p.seed, len(run),
+                                p.pre_walkers, p.pre_intervals, p.pre_iterations, p.intervals,
+                                p.walkers_per_interval, p.overlap, p.alpha, p.beta, p.iterations, p.exchange_every)
+            tot_ms += o["pre_ms"] + o["main_ms"]
+            done_groups += 1
+            if o["status"] == 0:
+                ok += len(run)
+                for k, q in enumerate(run):
+                    ref_out[q] = _reference_curve(o, k, p.X, p.Y, p.intervals)
+        res["reference_cuda"] = {"value": ok / (tot_ms / 1e3), "seconds": tot_ms / 1e3, "converged": ok,
+                                 "groups_run": done_groups, "groups": len(runs)}
+        outs["reference_cuda"] = ref_out
+    # accuracy on the same curves
+    acc = {k: [] for k in outs}
+    for run in _groups(probs[0]):
+        q = run[0]
+        p = probs[0][q]
+        if p.X > 12 or (p.X == 12 and p.boundary == 0):
+            continue
+        curves = {}
+        for k, o in outs.items():
+            if k == "reference_cuda":
+                curves[k] = o[q]
+            else:
+                r, E, G = o[q]
+                curves[k] = (E, G) if r.status == 0 else None
+        if any(v is None for v in curves.values()):
+            continue
+        for k, (E, G) in curves.items():
+            acc[k].append(_exact_rms(p, E, G)[0])
+    for k, v in acc.items():
+        res[k]["rms"] = float(np.mean(v)) if v else None
+        res[k]["curves"] = len(v)
+    res["workload"] = (f"{len(_groups(probs[0]))} groups (side x boundary x class) x {R} samples, p U[0.02,0.12] per "
+                       f"group, I=N/8 in [8,32], W=4, o=0.25, a=0.8, ln f 1e-6, exchange every 10")
+    if "reference_cuda" in res:
+        res["engine_x0_over_reference_cuda"] = res["engine_x0"]["value"] / res["reference_cuda"]["value"]
+    res["engine_over_plain"] = res["engine"]["value"] / res["plain"]["value"]
+    return res
+
+
+LARGE_CONV = dict(side=16, samples=1, classes="v", prob=0.10, seed=4343, beta=1e-5)
+
+
+def large_converged_run(side=None, samples=None, beta=None, classes=None):
+    """The large-lattice workload run to convergence on a bounded sample:
+    side x side periodic, p = 0.10, all four classes, 64 windows x 8 walkers,
+    overlap 0.3, exchange every 10.  This engine (exchange every 10, and
+    mode 0), the plain form and the reference's own kernels (one run per
+    class, no exchange) on the same problems; there is no exact density of
+    states at this size, so each arm's normalised log g is compared with the
+    reference kernels' on their common energies (RMS difference)."""
+    import qec_pf_wang_landau_gb300 as wlg
+    import oracle as O
+    c = dict(LARGE_CONV)
+    c.update({k: v for k, v in (("side", side), ("samples", samples), ("beta", beta), ("classes", classes))
+              if v is not None})
+    L, N = c["side"], c["side"] ** 2
+
+    def mk(m):
+        return [wlg.problem(L, L, prob=c["prob"], error_class=cl, seed=c["seed"], sample=k, pre_walkers=128,
+                            pre_intervals=128, pre_iterations=1000 * N, intervals=64, walkers_per_interval=8,
+                            overlap=0.3, alpha=0.8, beta=c["beta"], iterations=1000, exchange_every=10,
+                            exchange_mode=m) for cl in c["classes"] for k in range(c["samples"])]
+    probs = {m: mk(m) for m in (0, 1)}
+    ctx = wlg.Context(0)
+    res, curves = {}, {}
+    for m, name in ((1, "engine"), (0, "engine_x0")):
+        out = ctx.solve(probs[m])
+        st = ctx.stats()
+        ok = sum(1 for r, _, _ in out if r.status == 0)
+        res[name] = {"value": ok / ((st["pre_ms"] + st["handoff_ms"] + st["main_ms"]) / 1e3), "converged": ok,
+                     "main_ms": st["main_ms"], "outer_max": max(r.outer_iterations for r, _, _ in out)}
+        curves[name] = [(E, G) if r.status == 0 else None for r, E, G in out]
+    t0 = time.perf_counter()
+    out_p, _ = wlg.solve_plain(probs[0])
+    wall = time.perf_counter() - t0
+    ok = sum(1 for r, _, _ in out_p if r.status == 0)
+    res["plain"] = {"value": ok / wall, "seconds": wall, "converged": ok}
+    curves["plain"] = [(E, G) if r.status == 0 else None for r, E, G in out_p]
+    if O.reference_harness() is not None:
+        tot, ok, ref = 0.0, 0, []
+        for cl in c["classes"]:
+            o = O.reference_run(L, L, 0, c["prob"], cl, c["seed"], c["samples"], 128, 128, 1000 * N, 64, 8, 0.3, 0.8,
+                                c["beta"], 1000, 10)
+            tot += o["pre_ms"] + o["main_ms"]
+            ok += c["samples"] if o["status"] == 0 else 0
+            ref += [_reference_curve(o, k, L, L, 64) for k in range(c["samples"])]
+        res["reference_cuda"] = {"value": ok / (tot / 1e3), "seconds": tot / 1e3, "converged": ok}
+        for name in ("engine", "engine_x0", "plain"):
+            d = []
+            for a, b in zip(curves[name], ref):
+                if a is None or b is None:
+                    continue
+                common, ia, ib = np.intersect1d(a[0], b[0], return_indices=True)
+                d.append(float(np.sqrt(np.mean((a[1][ia] - b[1][ib]) ** 2))))
+            res[name]["rms_vs_reference"] = float(np.mean(d)) if d else None
+            res[name]["curves"] = len(d)
+        res["engine_x0_over_reference_cuda"] = res["engine_x0"]["value"] / res["reference_cuda"]["value"]
+    res["engine_over_plain"] = res["engine"]["value"] / res["plain"]["value"]
+    res["workload"] = (f"{L}x{L} periodic p={c['prob']}, {c['samples']} samples x classes {c['classes']}, I=64 W=8 "
+                       f"o=0.3 a=0.8, ln f {c['beta']:g}, exchange every 10, pre-run 128 x 1000 N")
     return res
 
 
@@ -497,12 +746,10 @@ def run_ours(args):
     single = ws == 1
     peaks, peak_kind = measured_peaks()
     achieved = BYTES_PER_FLIP * flips / max(t_main, 1e-12) / 1e9
-    plain_pps, plain_s, plain_launches = plain_run() if single else (None, None, None)
-    ref_cuda = reference_cuda_run() if single else None
-    cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1) if single else (None, None, 0.0)
+    value = converged / t_dev
     line = {
         "metric": METRIC,
-        "value": converged / t_dev,
+        "value": value,
         "unit": "samples/s",
         "n_gpus": ws,
         "steps": args.steps,
@@ -512,47 +759,79 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int32+f64",
-        "data": "synthetic: seeded Philox disorder (reference streams), no dataset",
-        "config": {"workload": "6x6 periodic, p=0.04, 100 disorder samples x classes ivhc, prerun 128w/32i/1000n, "
-                               "mainrun 10 windows x 3 walkers, o=0.25, alpha=0.8, ln f 1e-3, n=1000, exchange every 20",
-                   "problems_per_gpu": len(probs), "l2": "flushed between steps (512 MiB write)",
-                   "teams_per_cta": {f"form{t['form']}/team{t['team']}": t["per_cta"] for t in tuning}},
-        "flips_per_s": flips / t_main,
-        "converged": converged,
+        "data": "synthetic: seeded Philox disorder (reference streams)",
+        "config": {"workload": "6x6 periodic p=0.04, 100 samples x ivhc, prerun 128w/32i/1000n, mainrun I=10 W=3 "
+                               "o=0.25 a=0.8 ln f 1e-3 n=1000, exchange every 20",
+                   "problems_per_gpu": len(probs), "l2": "flushed between steps",
+                   "teams_per_cta": {f"f{t['form']}/t{t['team']}": t["per_cta"] for t in tuning}},
         "e2e": {"value": converged / t_e2e, "unit": "samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": MAIN_TRAFFIC_BYTES, "peak_kind": peak_kind,
-                     "basis": f"{BYTES_PER_FLIP} algorithmic B per WL flip of the main-run kernel, per launch / "
-                              "the launch's event-timed duration",
-                     "note": "walker state is on-chip (traffic 0.8 MB per launch against ~34 GB algorithmic); "
-                             "the step is one warp's dependent chain, 40% issue-active per warp"},
-        "cpu_baseline": {"value": cpu_pps, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
-                         "flips_per_s": cpu_fps,
-                         "sample": f"{CPU_SAMPLE_PROBLEMS} problems of the same workload (samples 0-23 x ivhc), "
-                                   f"{cpu_s:.1f} s wall"},
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": MAIN_TRAFFIC_BYTES,
+                     "peak_kind": peak_kind, "basis": f"{BYTES_PER_FLIP} B/flip"},
+        "flips_per_s": flips / t_main,
     }
-    line["plain"] = {"value": plain_pps, "unit": "samples/s", "seconds": plain_s, "kernel_launches": plain_launches,
-                     "what": "same 400 problems, reference structure on this engine's operator kernels "
-                             "(one launch per operation, host loop)"}
-    line["accuracy"] = accuracy(last_out, ref_cuda[2] if ref_cuda is not None else None)
-    if ref_cuda is not None:
-        line["reference_cuda"] = {"value": ref_cuda[0], "unit": "samples/s", "seconds": ref_cuda[1],
-                                  "what": "the reference's own kernels (unmodified wl.cu compiled for sm_103a) in its "
-                                          "prerun/mainrun order on this GB300; its exchange counter never "
-                                          "advances, so it runs without replica exchange at -c 20"}
     if clocks is not None:
-        line["clocks"] = clocks
-    if single:
-        line.update(secondary_ceilings(achieved, flips / t_main))
+        line["clocks"] = {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")}
     if not single:
-        for k in ("cpu_baseline", "plain", "accuracy"):
-            line.pop(k, None)
-    if not args.no_extra and single:
-        line["batched"] = batched_run()
-        line["large"] = large_run()
-        line["serving"] = serving_run()
-    return line
+        return r4(line)
+    cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1)
+    line["cpu_baseline"] = {"value": cpu_pps, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"{CPU_SAMPLE_PROBLEMS} problems (samples 0-23 x ivhc), {cpu_s:.1f} s"}
+    # comparison arms on the same 400 problems (samples/s, converged; device or wall time as stated)
+    plain_pps, plain_s, plain_launches = plain_run()
+    ref_cuda = reference_cuda_run()
+    x0_pps, x0_out = engine_x0_run(ctx, 3)
+    arms = {"plain": plain_pps, "engine_x0": x0_pps}
+    if ref_cuda is not None:
+        arms["reference_cuda"] = ref_cuda[0]
+        arms["x0_over_reference_cuda"] = x0_pps / ref_cuda[0]
+    arms["value_over_plain"] = value / plain_pps
+    line["arms"] = arms
+    line["accuracy"] = accuracy({"engine": last_out, "engine_x0": x0_out},
+                                ref_cuda[2] if ref_cuda is not None else None)
+    sec = secondary_ceilings(achieved, flips / t_main)
+    detail = {"plain": {"seconds": plain_s, "kernel_launches": plain_launches,
+                        "what": "same 400 problems, reference structure on this engine's operator kernels"},
+              "reference_cuda": None if ref_cuda is None else {
+                  "seconds": ref_cuda[1], "what": "the reference's own kernels (unmodified wl.cu for sm_103a) in its "
+                                                  "prerun/mainrun order; no exchange at -c 20 (its counter never "
+                                                  "advances)"},
+              "engine_x0": "this engine, exchange_mode 0 (the reference's behaviour at -c 20), device time",
+              **sec}
+    line["roofline_smem_frac"] = sec["roofline_smem"]["frac"]
+    if not args.no_extra:
+        legs = {"batched": batched_run(), "large": large_run(), "large_converged": large_converged_run(),
+                "serving": serving_run()}
+        detail.update(legs)
+        line["legs"] = legs_summary(legs)
+    print("detail " + json.dumps(r4(detail)), flush=True)
+    return r4(line)
+
+
+def legs_summary(legs):
+    """A few numbers per extra leg for the headline line."""
+    out = {}
+    b = legs.get("batched")
+    if b:
+        out["batched"] = {"value": b["value"], "ok": b["status_counts"].get("0", 0),
+                          "rms": {k: v["rms_mean"] for k, v in b["accuracy"].items()}}
+        for k in ("critical_path_ms", "main_ms", "arms"):
+            if k in b:
+                out["batched"][k] = b[k]
+    g = legs.get("large")
+    if g:
+        out["large"] = {k: v["flips_per_s"] for k, v in g.items() if isinstance(v, dict)}
+    c = legs.get("large_converged")
+    if c:
+        out["large_converged"] = {k: c[k]["value"] for k in ("engine", "engine_x0", "plain", "reference_cuda")
+                                  if k in c}
+        out["large_converged"]["rms_vs_ref"] = {k: c[k].get("rms_vs_reference") for k in ("engine", "engine_x0")}
+    v = legs.get("serving")
+    if v:
+        out["serving"] = {"ok": v["retired_ok"], "of": v["requests"], "readmitted": v["requests_readmitted"],
+                          "p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"]}
+    return out
 
 
 def secondary_ceilings(achieved_gbs, flips_per_s):
@@ -652,8 +931,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--profile-case", default=None, help="run a small fixed case for a profiler and exit")
-    ap.add_argument("--leg", default=None, choices=["serving", "batched", "large", "peaks"],
+    ap.add_argument("--leg", default=None, choices=["serving", "batched", "large", "c3_arms", "large_converged", "peaks"],
                     help="run one extra leg alone and print it")
+    ap.add_argument("--per-group", type=int, default=None, help="c3_arms: samples per group")
+    ap.add_argument("--sides", type=int, nargs="*", default=None, help="c3_arms: lattice sides")
+    ap.add_argument("--side", type=int, default=None, help="large_converged: lattice side")
+    ap.add_argument("--samples", type=int, default=None, help="large_converged: samples per class")
+    ap.add_argument("--beta", type=float, default=None, help="large_converged: final ln f")
+    ap.add_argument("--classes", default=None, help="large_converged: error classes, e.g. ivhc")
     ap.add_argument("--no-extra", action="store_true", help="skip the serving and batched legs")
     args = ap.parse_args()
     if args.profile_case:
@@ -663,8 +948,10 @@ def main():
         import qec_pf_wang_landau_gb300 as wlg
         wlg.build()
         legs = {"serving": serving_run, "batched": batched_run, "large": large_run,
+                "c3_arms": lambda: c3_arms_run(args.per_group, args.sides),
+                "large_converged": lambda: large_converged_run(args.side, args.samples, args.beta, args.classes),
                 "peaks": lambda: wlg.measure_peaks(0)}
-        print(json.dumps({args.leg: legs[args.leg]()}), flush=True)
+        print(json.dumps(r4({args.leg: legs[args.leg]()})), flush=True)
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:

@@ -322,6 +322,20 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
                        const signed char* lattices, double time_limit_s, wlg_result* results, int* energies,
                        double* log_g, long long capacity);
 
+/* The hand-off from pre-run to main run alone (file_io.cpp:558-659 with
+ * interval.cpp:5-41, as mainrun.cu:60-172 chains them), on the host: no
+ * device, no context.  Inputs as wlg_mainrun.  Per problem p, in problem
+ * order: status[p] (WLG_OK, or why its main run cannot start, e.g.
+ * WLG_ERR_NO_LATTICE); e_min[p], e_max[p], the visited energy range;
+ * spectrum[4N+1], 1 at every energy -2N + i the main run treats as
+ * reachable; win_start/win_end[intervals], the windows; start_lattices
+ * [intervals][N], each window's start lattice (spins +-1; every walker of
+ * the window starts from it).  Arrays are concatenated over problems. */
+wlg_status wlg_handoff(const wlg_problem* problems, int n, const unsigned char* seen, const signed char* couplings,
+                       const int* found, const int* found_energy, const signed char* lattices, int* status,
+                       int* e_min, int* e_max, unsigned char* spectrum, int* win_start, int* win_end,
+                       signed char* start_lattices);
+
 /* Plain form: the same problems computed with the reference's own structure
  * (prerun.cu:36-154, mainrun.cu:115-421) on the operators above — one
  * launch per operation, one thread per walker, state in global memory,
@@ -366,6 +380,15 @@ typedef struct {
 } wlg_stats;
 
 wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out);
+
+/* When the main run of each problem of the last wlg_solve / wlg_solve_raw
+ * on ctx started and finished, in milliseconds from the first problem's
+ * start, by the device clock (no counterpart in the reference, which runs
+ * every sample for the whole loop).  Problem order; -1 for problems that did
+ * not reach the main run.  *n_out = number of problems; WLG_ERR_CAPACITY
+ * when cap is smaller.  A batch's main-run time is at least its longest
+ * problem's end - start. */
+wlg_status wlg_last_main_times(const wlg_context* ctx, double* start_ms, double* end_ms, int cap, int* n_out);
 
 /* Secondary ceilings of the WL step on a device, measured by
  * microbenchmarks that fill every SM (no counterpart in the reference;
@@ -416,12 +439,16 @@ typedef struct {
   int max_resident;        /* resident problems (4 per request); 0: 8192 */
   int fail_after_epochs;   /* testing: a host-side failure is injected after this many epochs; 0: never */
   int stitching;           /* WLG_STITCH_REFERENCE (0) or WLG_STITCH_DEFINED */
+  int max_readmit;         /* re-admissions of a class whose pre-run missed part of the spectrum
+                              (WLG_ERR_NEW_ENERGY or WLG_ERR_NO_LATTICE), each with twice the
+                              previous pre-run iterations; 0: 4; negative: none (the class retires
+                              with that status, as the reference aborts its run) */
 } wlg_server_config;
 
 typedef struct {
   unsigned long long id;       /* as returned by wlg_server_submit */
   int status;                  /* WLG_OK, or the first failing class's status */
-  int pad;
+  int readmissions;            /* times some of its classes were re-admitted (max_readmit) */
   long long outer_iterations[4]; /* main-run outer iterations per class i, v, h, c */
   double log_z[4];             /* log Z_c at beta_N = ln((1-p)/p) / 2 */
   double log_probs[4];         /* log Z_c - logsumexp_c log Z_c */
@@ -431,6 +458,7 @@ typedef struct {
 typedef struct {
   long long submitted, completed, resident_problems, epochs, main_launches, prerun_launches;
   long long bytes_in_use, bytes_budget;
+  long long readmitted;        /* re-admissions (of one or more classes of a request) */
 } wlg_server_stats;
 
 wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_server** out);

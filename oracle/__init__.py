@@ -232,6 +232,8 @@ def reference_host():
         L.ref_interval.restype = C.c_int
         L.ref_stitch.argtypes = [P, i64, P, P, i32, i32, i32, i32, P, P, i32, P]
         L.ref_stitch.restype = C.c_int
+        L.ref_handoff.argtypes = [i32] * 6 + [f32] + [P] * 12 + [i64]
+        L.ref_handoff.restype = C.c_int
         _ref_host = L
     return _ref_host
 
@@ -326,3 +328,28 @@ def reference_mainrun(X, Y, boundary, seed, R, pre_i, seen, couplings, lattices,
             wins.append(raw[pos:pos + ln].copy())
             pos += ln
     return dict(status=st, main_ms=t_main.value, outer=outer.value, start=starts, end=ends, windows=wins)
+
+
+def ref_handoff(X, Y, R, pre_i, I, W, overlap, seen, found, found_energy, lattices):
+    """The reference's own hand-off (file_io.cpp:558-659 with interval.cpp, as
+    mainrun.cu chains them) on pre-run outputs of samples 0..R-1.  Returns None
+    when it throws, else dict(spectrum, off_spec, len_spec, e_min, e_max,
+    start, end, lattices [R*I*W][N])."""
+    L = reference_host()
+    N = X * Y
+    spec = np.zeros(R * (4 * N + 1), np.int8)
+    off = np.zeros(R, np.int32)
+    ln = np.zeros(R, np.int32)
+    lo = np.zeros(R, np.int32)
+    hi = np.zeros(R, np.int32)
+    s = np.zeros(R * I, np.int32)
+    e = np.zeros(R * I, np.int32)
+    lat = np.zeros(R * I * W * N, np.int8)
+    ins = [np.ascontiguousarray(seen, np.uint8), np.ascontiguousarray(found, np.int32),
+           np.ascontiguousarray(found_energy, np.int32), np.ascontiguousarray(lattices, np.int8)]
+    rc = L.ref_handoff(X, Y, R, pre_i, I, W, C.c_float(overlap), *(ptr(a) for a in ins), ptr(spec), ptr(off), ptr(ln),
+                       ptr(lo), ptr(hi), ptr(s), ptr(e), ptr(lat), len(spec))
+    if rc != 0:
+        return None
+    return dict(spectrum=spec[:int(ln.sum())], off_spec=off, len_spec=ln, e_min=lo, e_max=hi, start=s, end=e,
+                lattices=lat.reshape(R * I * W, N))

@@ -7,7 +7,9 @@
 * build_harness(): compiles oracle/ref_harness.cu (this project's own driver
   of those kernels) into oracle/_ref/libref_harness.so.
 * build_host(): compiles oracle/ref_host.cpp, which includes the reference's
-  unmodified src/interval.cpp and src/result_handling.cpp where they lie,
+  unmodified src/interval.cpp, src/result_handling.cpp and src/file_io.cpp
+  (the latter against the test-only HDF5 declarations of oracle/h5stub) where
+  they lie,
   into oracle/_ref/libref_host.so (host code; only where the reference
   sources exist, since the x86 library does not travel).
 """
@@ -50,16 +52,19 @@ def build_harness() -> str:
 
 
 def build_host() -> str | None:
-    srcs = [os.path.join(REFERENCE, "src", f) for f in ("interval.cpp", "result_handling.cpp")]
-    drv = os.path.join(HERE, "ref_host.cpp")
+    srcs = [os.path.join(REFERENCE, "src", f) for f in ("interval.cpp", "result_handling.cpp", "file_io.cpp")]
+    stub = os.path.join(HERE, "h5stub")
+    drv = [os.path.join(HERE, "ref_host.cpp"), os.path.join(stub, "hdf5.h"), os.path.join(stub, "h5stub.inc")]
     if not all(os.path.exists(f) for f in srcs):
         return None
     os.makedirs(OUT, exist_ok=True)
-    newest = max(os.path.getmtime(f) for f in srcs + [drv])
+    newest = max(os.path.getmtime(f) for f in srcs + drv)
     if os.path.exists(HOST) and os.path.getmtime(HOST) >= newest:
         return HOST
-    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-Wl,-Bsymbolic-functions",
-                    "-I" + os.path.join(REFERENCE, "src"), "-o", HOST + ".tmp", drv], check=True)
+    # the test-only HDF5 declarations come first on the include path: file_io.cpp
+    # is compiled for its in-memory hand-off functions only
+    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-Wl,-Bsymbolic-functions", "-I" + stub,
+                    "-I" + os.path.join(REFERENCE, "src"), "-o", HOST + ".tmp", drv[0]], check=True)
     os.replace(HOST + ".tmp", HOST)
     return HOST
 

@@ -52,6 +52,8 @@ SIGNATURES = {
     "wlg_couplings_from_syndrome": [i32, i32, i32, P, P],
     "wlg_solve_raw": [P, P, i32, P, P, P, P, i64, P],
     "wlg_last_stats": [P, P],
+    "wlg_last_main_times": [P, P, P, i32, P],
+    "wlg_handoff": [P, i32] + [P] * 12,
     "wlg_measure_peaks": [i32, P],
     "wlg_solve_plain": [P, i32, P, P, P, i64, P, P],
     "wlg_solve_raw_noalloc": [P, i32, P, P, P, P, i64, P, P],
@@ -279,6 +281,17 @@ class Context:
         call("wlg_last_stats", self._h, C.byref(st))
         return {f: getattr(st, f) for f, _ in Stats._fields_}
 
+    def main_times(self):
+        """Per problem of the last solve: (start_ms, end_ms) of its main run by
+        the device clock, from the first start; -1 where none ran."""
+        import numpy as np
+        k = i32(0)
+        lib().wlg_last_main_times(self._h, None, None, 0, C.byref(k))
+        a = np.zeros(max(k.value, 1))
+        b = np.zeros(max(k.value, 1))
+        call("wlg_last_main_times", self._h, a.ctypes.data_as(P), b.ctypes.data_as(P), k.value, C.byref(k))
+        return a[:k.value], b[:k.value]
+
 
 class Tuning(C.Structure):
     _fields_ = [("form", i32), ("team", i32), ("per_cta", i32), ("main_ms", f32), ("candidates", i32)]
@@ -299,6 +312,37 @@ def measure_peaks(device: int = 0):
     pk = Peaks()
     call("wlg_measure_peaks", device, C.byref(pk))
     return {f: getattr(pk, f) for f, _ in Peaks._fields_}
+
+
+def handoff(problems, seen, couplings, found, found_energy, lattices):
+    """wlg_handoff: the pre-run -> main-run hand-off on the host, from pre-run
+    outputs in wlg_prerun's layout.  Per problem: dict(status, e_min, e_max,
+    spectrum [4N+1], start [I], end [I], lattices [I][N])."""
+    import numpy as np
+    n = len(problems)
+    arr = (Problem * n)(*problems)
+    I = [p.intervals for p in problems]
+    N = [p.X * p.Y for p in problems]
+    st = np.zeros(n, np.int32)
+    lo = np.zeros(n, np.int32)
+    hi = np.zeros(n, np.int32)
+    spec = np.zeros(max(sum(4 * x + 1 for x in N), 1), np.uint8)
+    ws = np.zeros(max(sum(I), 1), np.int32)
+    we = np.zeros(max(sum(I), 1), np.int32)
+    lat = np.zeros(max(sum(i * x for i, x in zip(I, N)), 1), np.int8)
+    ins = [np.ascontiguousarray(seen, np.uint8), np.ascontiguousarray(couplings, np.int8),
+           np.ascontiguousarray(found, np.int32), np.ascontiguousarray(found_energy, np.int32),
+           np.ascontiguousarray(lattices, np.int8)]
+    call("wlg_handoff", C.cast(arr, P), n, *(a.ctypes.data_as(P) for a in ins), st.ctypes.data_as(P),
+         lo.ctypes.data_as(P), hi.ctypes.data_as(P), spec.ctypes.data_as(P), ws.ctypes.data_as(P),
+         we.ctypes.data_as(P), lat.ctypes.data_as(P))
+    out, os_, ow, ol = [], 0, 0, 0
+    for p in range(n):
+        out.append(dict(status=int(st[p]), e_min=int(lo[p]), e_max=int(hi[p]), spectrum=spec[os_:os_ + 4 * N[p] + 1],
+                        start=ws[ow:ow + I[p]], end=we[ow:ow + I[p]],
+                        lattices=lat[ol:ol + I[p] * N[p]].reshape(I[p], N[p])))
+        os_, ow, ol = os_ + 4 * N[p] + 1, ow + I[p], ol + I[p] * N[p]
+    return out
 
 
 def solve_plain(problems, stream=None):
@@ -336,18 +380,19 @@ def class_log_probs(curves, prob):
 
 class ServerConfig(C.Structure):
     _fields_ = [("mem_budget_bytes", sz), ("epoch_outer", i32), ("max_prerun_batch", i32), ("max_resident", i32),
-                ("fail_after_epochs", i32), ("stitching", i32)]
+                ("fail_after_epochs", i32), ("stitching", i32), ("max_readmit", i32)]
 
 
 class Decoded(C.Structure):
     """wlg_decoded: one retired request (classes in the order i, v, h, c)."""
-    _fields_ = [("id", u64), ("status", i32), ("pad", i32), ("outer_iterations", i64 * 4), ("log_z", f64 * 4),
+    _fields_ = [("id", u64), ("status", i32), ("readmissions", i32), ("outer_iterations", i64 * 4), ("log_z", f64 * 4),
                 ("log_probs", f64 * 4), ("submit_ms", f64), ("done_ms", f64)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", i64), ("completed", i64), ("resident_problems", i64), ("epochs", i64),
-                ("main_launches", i64), ("prerun_launches", i64), ("bytes_in_use", i64), ("bytes_budget", i64)]
+                ("main_launches", i64), ("prerun_launches", i64), ("bytes_in_use", i64), ("bytes_budget", i64),
+                ("readmitted", i64)]
 
 
 class Server:
@@ -355,8 +400,9 @@ class Server:
     poll retired requests with their four class log-probabilities."""
 
     def __init__(self, device: int = 0, mem_budget_bytes: int = 0, epoch_outer: int = 0, max_prerun_batch: int = 0,
-                 max_resident: int = 0, fail_after_epochs: int = 0, stitching: int = 0):
-        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident, fail_after_epochs, stitching)
+                 max_resident: int = 0, fail_after_epochs: int = 0, stitching: int = 0, max_readmit: int = 0):
+        cfg = ServerConfig(mem_budget_bytes, epoch_outer, max_prerun_batch, max_resident, fail_after_epochs, stitching,
+                           max_readmit)
         h = C.c_void_p()
         call("wlg_server_create", device, C.byref(cfg), C.byref(h))
         self._h = h

@@ -72,6 +72,9 @@ struct Exec {
   long long h2d = 0, d2h = 0;
   int launches = 0;
   int main_forms = 0;  // bit v: a main-run launch of form v
+  // per problem of the batch: when its main run started and ended (ms from
+  // the first start, device clock); -1 for problems without a main run
+  std::vector<double> p_start_ms, p_end_ms;
   std::string err;
   // teams per CTA chosen by an autotuner, by (form, team size); nullptr or
   // no entry: the built-in rule

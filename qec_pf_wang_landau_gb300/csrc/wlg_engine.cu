@@ -297,6 +297,42 @@ __device__ __forceinline__ int energy_after_flip(const Lat& l, uint64_t JR, uint
   return E + 2 * s * sigma;
 }
 
+// Energy after flipping `site` on the row layout (lattice_rows), the same
+// arithmetic as wl.cu:52-156: with r, ru, rd the rows of the site and of the
+// rows above and below, a bond is unsatisfied (s_a s_b J = -1) exactly when
+// the two spin bits and the coupling bit have odd parity, and flipping the
+// site changes the energy by 2 (deg - 2 unsat) over its deg bonds (4, or
+// fewer on an open edge, wl.cu:134-137).  Also returns the offset of the
+// site's row word and that word with the site flipped.
+__device__ __forceinline__ int energy_after_flip_rows(const Lat& l, const uint32_t* Jr_s, const uint32_t* Jd_s,
+                                                      int site, int E, const MainDesc& d, int& row_off,
+                                                      uint32_t& row_new)
+{
+  const int i = static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20);
+  const int j = site - i * d.Y;
+  const int iu = i == 0 ? d.X - 1 : i - 1;
+  const int id = i == d.X - 1 ? 0 : i + 1;
+  row_off = i * l.P;
+  const uint32_t r = l.s[row_off], ru = l.s[iu * l.P], rd = l.s[id * l.P];
+  const uint32_t mj = 1u << j;
+  const uint32_t mjl = j == 0 ? 1u << (d.Y - 1) : mj >> 1;
+  const uint32_t rr = (r >> 1) | ((r & 1u) << (d.Y - 1));  // bit c: spin (i, c + 1 mod Y)
+  const uint32_t h = r ^ rr ^ Jr_s[i];                     // bit c: bond (i, c)-(i, c + 1) unsatisfied
+  const uint32_t vu = (r ^ ru ^ Jd_s[iu]) & mj;            // bond (i - 1, j)-(i, j) unsatisfied
+  const uint32_t vd = (r ^ rd ^ Jd_s[i]) & mj;             // bond (i, j)-(i + 1, j) unsatisfied
+  row_new = r ^ mj;
+  int unsat, deg;
+  if (d.boundary == 0) {
+    unsat = __popc(h & (mj | mjl)) + __popc(vu) + __popc(vd);
+    deg = 4;
+  } else {
+    const uint32_t hm = (j < d.Y - 1 ? mj : 0u) | (j > 0 ? mjl : 0u);
+    unsat = __popc(h & hm) + (i > 0 ? __popc(vu) : 0) + (i < d.X - 1 ? __popc(vd) : 0);
+    deg = __popc(hm) + (i > 0 ? 1 : 0) + (i < d.X - 1 ? 1 : 0);
+  }
+  return E + 2 * (deg - 2 * unsat);
+}
+
 __device__ __forceinline__ bool mask_has(const uint32_t* mask, int c) { return (mask[c >> 5] >> (c & 31)) & 1u; }
 
 // Draws q and q + 1 of the words of A then B (q in [0, 3]); the three
@@ -308,6 +344,13 @@ __device__ __forceinline__ void pick_pair(const uint4& A, const uint4& B, int q,
   x2 = q3 ? B.x : (q2 ? A.w : (q1 ? A.z : A.y));
 }
 
+__device__ __forceinline__ long long device_clock_ns()
+{
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 template <bool kReg, bool kTable, bool kGlobalG>
 __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base, double* gslot,
                             const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
@@ -316,6 +359,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
                             unsigned char* __restrict__ statepool)
 {
   const int P = team.size;
+  const long long t_begin = t == 0 ? device_clock_ns() : 0;
   // resumable run: state saved at the end of a launch, restored at the start
   unsigned char* const st = d.off_state >= 0 ? statepool + d.off_state : nullptr;
   const StateLayout sl = state_layout(P, d.I, d.nwL, d.L);
@@ -545,12 +589,20 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         const bool need_site = act && ovr_site < 0 && (lo_s < d.site_thr || lo_s > ~d.site_thr);
         const int site = ovr_site >= 0 ? ovr_site : static_cast<int>(__umulhi(x1, nN));
         int En;
+        int row_off = 0;       // row layout: offset of the site's row word,
+        uint32_t row_new = 0;  // and that word with the site flipped
         if constexpr (kTable) {
           const ulonglong2 nt = nbt[site];
           const int unsat = __popcll((lt.r ^ nt.y) & nt.x);
           const int deg = __popcll(nt.x);
           const int sb = static_cast<int>((lt.r >> site) & 1ull);
           En = E + 2 * (1 - 2 * sb) * (deg - 2 * unsat);
+        } else if constexpr (!kReg) {
+          if (d.rows != 0) {
+            En = energy_after_flip_rows(lt, Jr_s, Jd_s, site, E, d, row_off, row_new);
+          } else {
+            En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
+          }
         } else {
           En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
         }
@@ -588,7 +640,15 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         }
         const bool commit = act && !need_site && !need_acc && !bad;
         const bool acc = commit && inside && (ovr_acc >= 0 ? ovr_acc != 0 : fast_acc);
-        flip_spin<kReg>(lt, site, acc);
+        if constexpr (!kReg) {
+          if (d.rows != 0) {
+            if (acc) lt.s[row_off] = row_new;
+          } else {
+            flip_spin<kReg>(lt, site, acc);
+          }
+        } else {
+          flip_spin<kReg>(lt, site, acc);
+        }
         E = acc ? En : E;
         // leaving c_cur: write back its log g, shadow and visit count
         const bool chg = acc && !same;
@@ -802,6 +862,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
       r.outer = outer;
       r.flips = outer * static_cast<long long>(d.nwalk) * d.n_iter;
       r.done = 0;
+      r.t_start = t_begin;
+      r.t_end = device_clock_ns();
       results[p] = r;
     }
     team.sync();
@@ -819,6 +881,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
     r.outer = outer;
     r.flips = outer * static_cast<long long>(d.nwalk) * d.n_iter;
     r.done = 1;
+    r.t_start = t_begin;
+    r.t_end = device_clock_ns();
     results[p] = r;
   }
   team.sync();

@@ -38,6 +38,27 @@ struct PreDesc {
 };
 
 // ----------------------------------------------------------- main run -----
+// Bit-packed lattices and couplings.  Lattices of more than 64 sites whose
+// rows fit a 32-bit word (2 <= Y <= 32) are kept one row per word: bit j of
+// word i is site (i, j), so a site's four neighbours lie in three words
+// (its row and the rows above and below).  Others are packed linearly: bit
+// q & 31 of word q >> 5 is site q = i*Y + j.  A set bit is a -1 spin or a
+// -1 coupling; right bonds (site, site + 1 in the row) and down bonds (site,
+// site + Y) are packed the same way as the sites that own them.
+WLG_HD inline bool lattice_rows(int X, int Y) { return X * Y > 64 && Y >= 2 && Y <= 32; }
+WLG_HD inline int lattice_words(int X, int Y) { return lattice_rows(X, Y) ? X : (X * Y + 31) / 32; }
+// word and bit of site q (q = i*Y + j)
+WLG_HD inline void lattice_bit(int X, int Y, int q, int& word, int& bit)
+{
+  if (lattice_rows(X, Y)) {
+    word = q / Y;
+    bit = q - word * Y;
+  } else {
+    word = q >> 5;
+    bit = q & 31;
+  }
+}
+
 // One team of threads per problem (one thread per walker, team size a
 // multiple of 32).  Walker state lives in registers and the team's shared
 // memory for the whole run.
@@ -54,7 +75,8 @@ struct MainDesc {
   uint32_t site_thr;             // 2^32 * (N 2^-21 + 2^-18): site pick needs the exact path within this
   double site_scale;             // (N - 1) + 0.999999, wl.cu:64
   long long max_outer;           // 0 = no cap
-  int nwL;                       // 32-bit words per lattice
+  int nwL;                       // 32-bit words per lattice (lattice_words)
+  int rows;                      // 1: one row per word (lattice_rows)
   int nwM;                       // 32-bit words of the compact spectrum mask
   long long off_J;               // words: right bonds [nwL], down bonds [nwL]
   long long off_lat;             // words: start lattice of each window [I][nwL]
@@ -73,6 +95,9 @@ struct MainResult {
   long long flips;
   int done;    // 1: finished (status final, log g written); 0: suspended
   int pad;
+  // device clock (%globaltimer, ns) when this launch started the problem and
+  // when it finished or suspended it
+  long long t_start, t_end;
 };
 
 // Saved state of a suspended problem (resumable runs), byte offsets: a

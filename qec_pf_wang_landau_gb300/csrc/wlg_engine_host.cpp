@@ -270,6 +270,7 @@ struct wlg_context {
   long long h2d = 0, d2h = 0;
   int launches = 0;
   int main_forms = 0;
+  std::vector<double> p_start_ms, p_end_ms;  // of the last solve, per problem
   std::map<std::pair<int, int>, int> tuned;  // teams per CTA by (form, team size), from wlg_context_autotune
   int stitching = WLG_STITCH_REFERENCE;
   std::string err;
@@ -524,7 +525,7 @@ void handoff_one(const wlg_problem& q, const PreDesc& a, const PreOut& po, Hando
   std::map<int, int> by_energy;
   for (int k = 0; k < a.n_int; ++k)
     if (fflag[a.off_fflag + k] != 0) by_energy.emplace(fflag[a.off_fflag + a.n_int + k], k);
-  const int nwL = (N + 31) / 32;
+  const int nwL = wlg::lattice_words(q.X, q.Y);
   std::vector<int> pick(static_cast<size_t>(q.intervals), -1), E0(static_cast<size_t>(q.intervals));
   bool ok = true;
   for (int b = 0; b < q.intervals && ok; ++b) {
@@ -573,6 +574,7 @@ void handoff_one(const wlg_problem& q, const PreDesc& a, const PreOut& po, Hando
   d.site_thr = static_cast<uint32_t>(N) * 2048u + 16384u;
   d.max_outer = q.max_outer;
   d.nwL = nwL;
+  d.rows = wlg::lattice_rows(q.X, q.Y) ? 1 : 0;
   const int nbins = (e_hi - e_lo) / g + 1;
   d.nwM = (nbins + 31) / 32;
   // windows: start, end, compact base (first energy >= start on the lattice
@@ -586,15 +588,19 @@ void handoff_one(const wlg_problem& q, const PreDesc& a, const PreOut& po, Hando
     L = std::max(L, len[b]);
   }
   d.L = L;
-  for (int half = 0; half < 2; ++half)
-    for (int wd = 0; wd < nwL; ++wd) {
-      uint32_t v = 0;
-      for (int bit = 0; bit < 32; ++bit) {
-        const int q2 = wd * 32 + bit;
-        if (q2 < N && J8[a.off_J + half * N + q2] == -1) v |= 1u << bit;
-      }
-      out.Jw.push_back(v);
+  // bit-packed couplings (right bonds, then down bonds) and lattices in the
+  // layout of lattice_bit
+  auto pack = [&](const int8_t* v, std::vector<uint32_t>& dst) {
+    const size_t at = dst.size();
+    dst.resize(at + static_cast<size_t>(nwL), 0u);
+    for (int s = 0; s < N; ++s) {
+      int wd = 0, bit = 0;
+      wlg::lattice_bit(q.X, q.Y, s, wd, bit);
+      if (v[s] == -1) dst[at + static_cast<size_t>(wd)] |= 1u << bit;
     }
+  };
+  pack(J8.data() + a.off_J, out.Jw);
+  pack(J8.data() + a.off_J + N, out.Jw);
   for (int b = 0; b < d.I; ++b) {
     const int8_t* src = found.data() + a.off_found + static_cast<long long>(pick[b]) * N;
     if (wlg::energy_host(src, J8.data() + a.off_J, q.X, q.Y, q.boundary) != E0[b]) {
@@ -602,14 +608,7 @@ void handoff_one(const wlg_problem& q, const PreDesc& a, const PreOut& po, Hando
       out.why = "stored lattice energy mismatch";
       return;
     }
-    for (int wd = 0; wd < nwL; ++wd) {
-      uint32_t v = 0;
-      for (int bit = 0; bit < 32; ++bit) {
-        const int q2 = wd * 32 + bit;
-        if (q2 < N && src[q2] == -1) v |= 1u << bit;
-      }
-      out.latw.push_back(v);
-    }
+    pack(src, out.latw);
   }
   std::vector<int>& win = out.win;
   win.insert(win.end(), ws.begin(), ws.end());
@@ -724,6 +723,12 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
   // ---------------- main run: one persistent launch per (lattice storage, team size)
   const int m = static_cast<int>(prep.main.size());
   mres.assign(static_cast<size_t>(m), MainResult{});
+  // per problem of the batch (a sub-batch, as the autotuner runs, lists only
+  // its main-run problems)
+  size_t n_prob = prep.starts.size();
+  for (const int p : prep.main_problem) n_prob = std::max(n_prob, static_cast<size_t>(p) + 1);
+  ex.p_start_ms.assign(n_prob, -1.0);
+  ex.p_end_ms.assign(n_prob, -1.0);
   out_host.assign(static_cast<size_t>(o_out), 0.0);
   win_host = win;
   if (m == 0) return WLG_OK;
@@ -732,10 +737,21 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
   // one launch per (form, team size); the form by lattice storage (fit_form)
   std::map<std::pair<int, int>, std::vector<int>> groups;
   for (int i = 0; i < m; ++i) groups[{wlg::fit_form(prep.main[i], prep.main[i].team), prep.main[i].team}].push_back(i);
+  // Longest problems first (larger lattices take more outer iterations of
+  // longer steps): the groups' launches are issued, and each group's queue
+  // is ordered, by decreasing lattice size, so the batch's longest serial
+  // chains start at once instead of waiting for SMs held by shorter ones.
+  // Results do not depend on the order (every problem's trajectory is its own).
+  std::vector<std::pair<std::pair<int, int>, std::vector<int>>> ordered(groups.begin(), groups.end());
+  for (auto& [key, idx] : ordered)
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return prep.main[a].N > prep.main[b].N; });
+  std::stable_sort(ordered.begin(), ordered.end(), [&](const auto& a, const auto& b) {
+    return prep.main[a.second.front()].N > prep.main[b.second.front()].N;
+  });
   std::vector<int> order;
   // variant, team, bytes, per_cta, first, count, L (max compact bins)
   std::vector<std::tuple<int, int, int, int, int, int, int>> launches;
-  for (const auto& [key, idx] : groups) {
+  for (const auto& [key, idx] : ordered) {
     const int variant = key.first;
     const int team = key.second;
     int bytes = 0;
@@ -863,6 +879,12 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
     for (int i = 0; i < m; ++i)
       if (last[i].status == WLG_ERR_TIMEOUT && last[i].done == 0) mres[i].status = WLG_ERR_TIMEOUT;
   if (ex.ev != nullptr) cudaEventElapsedTime(&ex.t_main, ex.ev[2], ex.ev[3]);
+  long long t_first = 0;
+  for (int i = 0; i < m; ++i) t_first = i == 0 ? mres[i].t_start : std::min(t_first, mres[i].t_start);
+  for (int i = 0; i < m; ++i) {
+    ex.p_start_ms[prep.main_problem[i]] = 1e-6 * static_cast<double>(mres[i].t_start - t_first);
+    ex.p_end_ms[prep.main_problem[i]] = 1e-6 * static_cast<double>(mres[i].t_end - t_first);
+  }
   for (int i = 0; i < m; ++i) {
     wlg_result& r = results[prep.main_problem[i]];
     r.status = mres[i].status;
@@ -894,12 +916,56 @@ void keep_stats(wlg_context* ctx, const Exec& ex)
   ctx->d2h = ex.d2h;
   ctx->launches = ex.launches;
   ctx->main_forms = ex.main_forms;
+  ctx->p_start_ms = ex.p_start_ms;
+  ctx->p_end_ms = ex.p_end_ms;
   if (!ex.err.empty()) ctx->err = ex.err;
 }
 
 wlg_status raw_windows(Exec& ex, const wlg_problem* problems, int n, const Prepared& prep,
                        const std::vector<double>& out, const std::vector<int>& win, int* win_start, int* win_end,
                        double* raw_log_g, long long raw_capacity, long long* raw_offset);
+
+// Pre-run outputs given by the caller (the layout wlg_prerun writes) as the
+// hand-off's input; WLG_ERR_INVALID when couplings or stored lattices are
+// not +-1.
+wlg_status given_prerun(const wlg_problem* problems, int n, wlg_result* results, const unsigned char* seen,
+                        const signed char* couplings, const int* found, const int* found_energy,
+                        const signed char* lattices, PreOut& po, std::string& err)
+{
+  int threads = 0, smem = 0;
+  wlg_status st = prerun_descs(problems, n, results, po, threads, smem, err);
+  if (st != WLG_OK) return st;
+  long long ob = 0;
+  auto pm1 = [](const signed char* v, long long m) {
+    for (long long i = 0; i < m; ++i)
+      if (v[i] != 1 && v[i] != -1) return false;
+    return true;
+  };
+  for (int p = 0; p < n; ++p) {
+    const PreDesc& d = po.pd[p];
+    bool valid = pm1(couplings + d.off_J, 2LL * d.N);
+    for (int b = 0; b < d.n_int && valid; ++b)
+      valid = found[ob + b] == 0 || pm1(lattices + d.off_found + static_cast<long long>(b) * d.N, d.N);
+    if (!valid) {
+      err = "couplings or stored lattice of problem " + std::to_string(p) + " not +-1";
+      return WLG_ERR_INVALID;
+    }
+    std::memcpy(po.seen.data() + d.off_seen, seen + d.off_seen, static_cast<size_t>(4 * d.N + 1));
+    std::memcpy(po.J8.data() + d.off_J, couplings + d.off_J, static_cast<size_t>(2 * d.N));
+    std::memcpy(po.found.data() + d.off_found, lattices + d.off_found, static_cast<size_t>(d.n_int) * d.N);
+    for (int b = 0; b < d.n_int; ++b) {
+      po.fflag[d.off_fflag + b] = found[ob + b];
+      po.fflag[d.off_fflag + d.n_int + b] = found_energy[ob + b];
+    }
+    ob += d.n_int;
+  }
+  return WLG_OK;
+}
+
+// An Exec for host-only phases: it hands out no device buffers.
+struct HostExec final : Exec {
+  wlg_status buffer(Slot, size_t, void**) override { return WLG_ERR_INVALID; }
+};
 
 // Dense walker-0 log g of window b (zeros where the lattice cannot reach).
 void dense_window(const MainDesc& d, const std::vector<double>& out, const std::vector<int>& win, int b,
@@ -1145,36 +1211,11 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
     ex.t_pre = ex.t_main = 0;
     ex.t_handoff = 0;
     PreOut po;
-    int threads = 0, smem = 0;
     std::string err;
-    wlg_status st = prerun_descs(problems, n, results, po, threads, smem, err);
+    wlg_status st = given_prerun(problems, n, results, seen, couplings, found, found_energy, lattices, po, err);
     if (st != WLG_OK) {
       ctx->err = err;
       return st;
-    }
-    long long ob = 0;
-    auto pm1 = [](const signed char* v, long long m) {
-      for (long long i = 0; i < m; ++i)
-        if (v[i] != 1 && v[i] != -1) return false;
-      return true;
-    };
-    for (int p = 0; p < n; ++p) {
-      const PreDesc& d = po.pd[p];
-      bool valid = pm1(couplings + d.off_J, 2LL * d.N);
-      for (int b = 0; b < d.n_int && valid; ++b)
-        valid = found[ob + b] == 0 || pm1(lattices + d.off_found + static_cast<long long>(b) * d.N, d.N);
-      if (!valid) {
-        ctx->err = "couplings or stored lattice of problem " + std::to_string(p) + " not +-1";
-        return WLG_ERR_INVALID;
-      }
-      std::memcpy(po.seen.data() + d.off_seen, seen + d.off_seen, static_cast<size_t>(4 * d.N + 1));
-      std::memcpy(po.J8.data() + d.off_J, couplings + d.off_J, static_cast<size_t>(2 * d.N));
-      std::memcpy(po.found.data() + d.off_found, lattices + d.off_found, static_cast<size_t>(d.n_int) * d.N);
-      for (int b = 0; b < d.n_int; ++b) {
-        po.fflag[d.off_fflag + b] = found[ob + b];
-        po.fflag[d.off_fflag + d.n_int + b] = found_energy[ob + b];
-      }
-      ob += d.n_int;
     }
     Prepared prep;
     Handoff ho;
@@ -1186,6 +1227,66 @@ wlg_status wlg_mainrun(wlg_context* ctx, const wlg_problem* problems, int n, con
     keep_stats(ctx, ex);
     if (st != WLG_OK) return st;
     return stitch_all(ctx, prep, out, win, results, energies, log_g, capacity);
+  });
+}
+
+wlg_status wlg_handoff(const wlg_problem* problems, int n, const unsigned char* seen, const signed char* couplings,
+                       const int* found, const int* found_energy, const signed char* lattices, int* status,
+                       int* e_min, int* e_max, unsigned char* spectrum, int* win_start, int* win_end,
+                       signed char* start_lattices)
+{
+  return wlg::guarded([&]() -> wlg_status {
+    if (n < 0 || (n > 0 && (problems == nullptr || seen == nullptr || couplings == nullptr || found == nullptr ||
+                            found_energy == nullptr || lattices == nullptr || status == nullptr || e_min == nullptr ||
+                            e_max == nullptr || spectrum == nullptr || win_start == nullptr || win_end == nullptr ||
+                            start_lattices == nullptr)))
+      return WLG_ERR_INVALID;
+    std::vector<wlg_result> res(static_cast<size_t>(n));
+    PreOut po;
+    std::string err;
+    wlg_status st = given_prerun(problems, n, res.data(), seen, couplings, found, found_energy, lattices, po, err);
+    if (st != WLG_OK) return st;
+    HostExec ex;
+    Prepared prep;
+    Handoff ho;
+    if ((st = handoff(ex, problems, n, res.data(), po, prep, ho)) != WLG_OK) return st;
+    std::vector<int> main_of(static_cast<size_t>(n), -1);
+    for (size_t i = 0; i < prep.main.size(); ++i) main_of[prep.main_problem[i]] = static_cast<int>(i);
+    long long ow = 0, ol = 0, os = 0;
+    for (int p = 0; p < n; ++p) {
+      const wlg_problem& q = problems[p];
+      const int N = q.X * q.Y, I = q.intervals;
+      std::fill(spectrum + os, spectrum + os + 4 * N + 1, 0);
+      std::fill(win_start + ow, win_start + ow + I, 0);
+      std::fill(win_end + ow, win_end + ow + I, 0);
+      std::fill(start_lattices + ol, start_lattices + ol + static_cast<long long>(I) * N, 0);
+      e_min[p] = e_max[p] = 0;
+      if (main_of[p] < 0) {
+        status[p] = res[p].status != WLG_OK ? res[p].status : WLG_ERR_NO_LATTICE;
+      } else {
+        const MainDesc& d = prep.main[main_of[p]];
+        status[p] = WLG_OK;
+        e_min[p] = d.e_min;
+        e_max[p] = d.e_max;
+        const int g = 1 << d.lg;
+        for (int c = 0; c * g <= d.e_max - d.e_min; ++c)
+          if ((ho.maskw[d.off_mask + (c >> 5)] >> (c & 31)) & 1u) spectrum[os + d.e_min + c * g + 2 * N] = 1;
+        for (int b = 0; b < I; ++b) {
+          win_start[ow + b] = ho.win[d.off_win + b];
+          win_end[ow + b] = ho.win[d.off_win + I + b];
+          const uint32_t* w = ho.latw.data() + d.off_lat + static_cast<long long>(b) * d.nwL;
+          for (int s = 0; s < N; ++s) {
+            int wd = 0, bit = 0;
+            wlg::lattice_bit(q.X, q.Y, s, wd, bit);
+            start_lattices[ol + static_cast<long long>(b) * N + s] = ((w[wd] >> bit) & 1u) ? -1 : 1;
+          }
+        }
+      }
+      ow += I;
+      ol += static_cast<long long>(I) * N;
+      os += 4 * N + 1;
+    }
+    return WLG_OK;
   });
 }
 
@@ -1265,6 +1366,19 @@ wlg_status wlg_last_stats(const wlg_context* ctx, wlg_stats* out)
   out->d2h_bytes = ctx->d2h;
   out->kernel_launches = ctx->launches;
   out->main_forms = ctx->main_forms;
+  return WLG_OK;
+}
+
+wlg_status wlg_last_main_times(const wlg_context* ctx, double* start_ms, double* end_ms, int cap, int* n_out)
+{
+  if (ctx == nullptr || n_out == nullptr || cap < 0) return WLG_ERR_INVALID;
+  const int n = static_cast<int>(ctx->p_start_ms.size());
+  *n_out = n;
+  if (cap < n) return WLG_ERR_CAPACITY;
+  for (int i = 0; i < n; ++i) {
+    if (start_ms != nullptr) start_ms[i] = ctx->p_start_ms[i];
+    if (end_ms != nullptr) end_ms[i] = ctx->p_end_ms[i];
+  }
   return WLG_OK;
 }
 
@@ -1352,7 +1466,7 @@ size_t noalloc_bound(const wlg_problem* probs, int n)
   for (int p = 0; p < n; ++p) {
     const wlg_problem& q = probs[p];
     const size_t N = static_cast<size_t>(q.X) * q.Y, I = static_cast<size_t>(q.intervals);
-    const size_t nwL = (N + 31) / 32, nbins = 2 * N + 1;
+    const size_t nwL = static_cast<size_t>(wlg::lattice_words(q.X, q.Y)), nbins = 2 * N + 1;
     MainDesc d{};
     d.X = q.X;
     d.Y = q.Y;

@@ -37,6 +37,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <bit>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -179,7 +180,7 @@ BlockLayout block_bound(const wlg_problem& q)
     for (int b = 0; b < q.intervals; ++b) L = std::max(L, (e[b] - s[b]) / 2 + 1);
   }
   const int nbins = 2 * N + 1;
-  return block_layout(round32(q.intervals * q.walkers_per_interval), q.intervals, L, (N + 31) / 32,
+  return block_layout(round32(q.intervals * q.walkers_per_interval), q.intervals, L, lattice_words(q.X, q.Y),
                       (nbins + 31) / 32);
 }
 
@@ -201,8 +202,13 @@ struct Request {
   std::vector<int8_t> J;  // given class-'i' couplings (2N), empty: drawn
   wlg_decoded out{};
   int remaining = kClasses;
+  unsigned todo = (1u << kClasses) - 1;  // classes of the next admission
+  unsigned retry = 0;                    // classes to re-admit once every class of this admission is done
+  int pre_iterations[kClasses] = {};     // per class; 0: q.pre_iterations
+  int attempts[kClasses] = {};           // re-admissions so far, per class
   int status[kClasses] = {};
   std::vector<std::pair<int, double>> curve[kClasses];
+  int pre_iter(int c) const { return pre_iterations[c] > 0 ? pre_iterations[c] : q.pre_iterations; }
 };
 
 struct Epoch {
@@ -230,6 +236,7 @@ struct Group {
 // hand-off) by the admission thread while the loop keeps launching epochs.
 struct AdmitJob {
   std::vector<std::pair<unsigned long long, Request>> batch;
+  std::vector<std::pair<int, int>> who;  // per problem: (index in batch, class)
   std::vector<size_t> block_off;
   std::vector<BlockLayout> bound;
   std::vector<wlg_problem> qs;
@@ -435,10 +442,36 @@ void wlg_server::class_done(unsigned long long id, int cls, int status, long lon
   r.status[cls] = status;
   r.out.outer_iterations[cls] = outer;
   r.curve[cls] = std::move(curve);
-  if (--r.remaining == 0) {
-    complete(id, r);
+  // A class whose pre-run missed part of the spectrum (a walker later found a
+  // new energy, or a window got no start lattice) is re-admitted with twice
+  // the pre-run iterations: a deterministic function of the request, so the
+  // result equals the batch engine's for that larger pre-run.  (The
+  // reference aborts the whole run instead.)
+  if ((status == WLG_ERR_NEW_ENERGY || status == WLG_ERR_NO_LATTICE) && r.attempts[cls] < cfg.max_readmit)
+    r.retry |= 1u << cls;
+  if (--r.remaining > 0) return;
+  if (r.retry != 0) {
+    for (int c = 0; c < kClasses; ++c)
+      if ((r.retry >> c) & 1u) {
+        r.pre_iterations[c] = std::min(2 * static_cast<long long>(r.pre_iter(c)), 1ll << 30);
+        r.attempts[c] += 1;
+        r.status[c] = WLG_OK;
+        r.curve[c].clear();
+      }
+    r.todo = r.retry;
+    r.remaining = std::popcount(r.retry);
+    r.retry = 0;
+    r.out.readmissions += 1;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      ++stats.readmitted;
+    }
+    pending.emplace_front(id, std::move(r));
     active.erase(it);
+    return;
   }
+  complete(id, r);
+  active.erase(it);
 }
 
 // Pending requests -> reserved arena blocks -> the admission thread; a
@@ -465,12 +498,14 @@ bool wlg_server::admit()
   std::vector<BlockLayout>& bound = nj->bound;
   while (!pending.empty() && static_cast<int>(batch.size()) < cfg.max_prerun_batch &&
          static_cast<int>(free_slots.size()) >= kClasses * static_cast<int>(batch.size() + 1)) {
-    const BlockLayout bl = block_bound(pending.front().second.q);
+    const Request& front = pending.front().second;
+    const BlockLayout bl = block_bound(front.q);
+    const int nc = std::popcount(front.todo);
     size_t offs[kClasses];
     int got = 0;
-    for (; got < kClasses; ++got)
+    for (; got < nc; ++got)
       if (!arena.alloc(bl.bytes, &offs[got])) break;
-    if (got < kClasses) {
+    if (got < nc) {
       for (int c = 0; c < got; ++c) arena.release(offs[c], bl.bytes);
       if (active.empty() && batch.empty() && reclaim.empty()) {  // can never fit
         auto [id, r] = std::move(pending.front());
@@ -486,34 +521,37 @@ bool wlg_server::admit()
       }
       break;
     }
-    for (int c = 0; c < kClasses; ++c) {
-      block_off.push_back(offs[c]);
-      bound.push_back(bl);
-    }
+    for (int c = 0, j = 0; c < kClasses; ++c)
+      if ((front.todo >> c) & 1u) {
+        block_off.push_back(offs[j++]);
+        bound.push_back(bl);
+        nj->who.emplace_back(static_cast<int>(batch.size()), c);
+      }
     batch.push_back(std::move(pending.front()));
     pending.pop_front();
   }
   if (batch.empty()) return any;
-  const int n = static_cast<int>(batch.size()) * kClasses;
+  const int n = static_cast<int>(nj->who.size());
   nj->qs.resize(static_cast<size_t>(n));
-  for (size_t i = 0; i < batch.size(); ++i)
-    for (int c = 0; c < kClasses; ++c) {
-      nj->qs[i * kClasses + c] = batch[i].second.q;
-      nj->qs[i * kClasses + c].error_class = kClassName[c];
-    }
+  for (int k = 0; k < n; ++k) {
+    const auto [i, c] = nj->who[k];
+    const Request& r = batch[i].second;
+    nj->qs[k] = r.q;
+    nj->qs[k].error_class = kClassName[c];
+    nj->qs[k].pre_iterations = r.pre_iter(c);
+  }
   bool any_given = false;
   for (const auto& [id, r] : batch) any_given |= !r.J.empty();
   if (any_given)
-    for (size_t i = 0; i < batch.size(); ++i)
-      for (int c = 0; c < kClasses; ++c) {
-        const Request& r = batch[i].second;
-        const size_t twoN = 2 * static_cast<size_t>(r.q.X) * r.q.Y;
-        if (r.J.empty())
-          nj->J.insert(nj->J.end(), twoN, 1);
-        else
-          nj->J.insert(nj->J.end(), r.J.begin(), r.J.end());
-        nj->given.push_back(r.J.empty() ? 0 : 1);
-      }
+    for (int k = 0; k < n; ++k) {
+      const Request& r = batch[nj->who[k].first].second;
+      const size_t twoN = 2 * static_cast<size_t>(r.q.X) * r.q.Y;
+      if (r.J.empty())
+        nj->J.insert(nj->J.end(), twoN, 1);
+      else
+        nj->J.insert(nj->J.end(), r.J.begin(), r.J.end());
+      nj->given.push_back(r.J.empty() ? 0 : 1);
+    }
   nj->res.resize(static_cast<size_t>(n));
   job = std::move(nj);
   {
@@ -579,8 +617,8 @@ void wlg_server::finish_admission(AdmitJob& aj)
   admit_ev.push_back(ev);
   std::vector<unsigned char> host;
   for (int k = 0; k < n; ++k) {
-    const unsigned long long id = batch[k / kClasses].first;
-    const int cls = k % kClasses;
+    const unsigned long long id = batch[aj.who[k].first].first;
+    const int cls = aj.who[k].second;
     const size_t boff = block_off[k];
     const BlockLayout& bb = bound[k];
     if (main_of[k] < 0) {  // no main run (no lattice for a window, empty window, ...)
@@ -865,6 +903,8 @@ wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_se
     if (s->cfg.mem_budget_bytes == 0) s->cfg.mem_budget_bytes = size_t{1} << 30;
     if (s->cfg.epoch_outer <= 0) s->cfg.epoch_outer = 4;
     if (s->cfg.max_prerun_batch <= 0) s->cfg.max_prerun_batch = 256;
+    if (s->cfg.max_readmit == 0) s->cfg.max_readmit = 4;
+    if (s->cfg.max_readmit < 0) s->cfg.max_readmit = 0;
     if (s->cfg.max_resident <= 0) s->cfg.max_resident = 8192;
     if (s->cfg.max_resident < kClasses) return WLG_ERR_INVALID;
     if (s->cfg.stitching != WLG_STITCH_REFERENCE && s->cfg.stitching != WLG_STITCH_DEFINED) return WLG_ERR_INVALID;

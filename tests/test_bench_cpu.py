@@ -63,11 +63,18 @@ def test_accuracy_scores_exact_curves_as_exact():
             E = (np.nonzero(cnt)[0] - 2 * N).astype(np.int32)
             out.append((types.SimpleNamespace(status=0), E, np.log(cnt[E + 2 * N]) + 1e-3))
     out[5] = (types.SimpleNamespace(status=3), np.zeros(0, np.int32), np.zeros(0))  # sample 1, class v
-    acc = bench.accuracy(out, None)
-    assert acc["engine_energy_sets_exact"] and abs(acc["engine"]["rms_mean"] - 1e-3) < 1e-9
-    d = acc["class_decisions"]
-    assert d["samples"] == 100 and d["engine_equals_exact"] == 99 and d["reference_cuda_equals_exact"] == 0
-    assert sum(d["exact_classes"].values()) == 100
+    acc = bench.accuracy({"engine": out, "engine_x0": out[:5] + out[5:]}, None)
+    assert acc["engine_sets_exact"] and abs(acc["rms"]["engine"] - 1e-3) < 1e-9
+    assert acc["rms"]["engine_x0"] == acc["rms"]["engine"] and "reference_cuda" not in acc["rms"]
+    d = acc["class_decisions_equal_exact"]
+    assert acc["samples"] == 100 and d["engine"] == 99 and d["engine_x0"] == 99 and d["reference_cuda"] == 0
+    assert sum(acc["exact_class_counts"].values()) == 100
+
+
+def test_r4_shortens_numbers_only():
+    import bench
+    assert bench.r4({"a": 1234.5678, "b": [0.000123456, 3, "x"], "c": float("nan")}) == \
+        {"a": 1235.0, "b": [0.0001235, 3, "x"], "c": None}
 
 
 def test_batched_accuracy_scores_every_side_against_exact():

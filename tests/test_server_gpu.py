@@ -35,19 +35,37 @@ def mixed_requests(wlg, n):
     return out
 
 
-def batch_reference(wlg, ctx, req):
-    """The four class problems through the batch engine + class probabilities."""
-    probs = []
-    for c in CLASSES:
-        q = wlg.Problem.from_buffer_copy(req)
-        q.error_class = c.encode()
-        probs.append(q)
-    out = ctx.solve(probs)
+MISSED = (3, 5)  # WLG_ERR_NEW_ENERGY, WLG_ERR_NO_LATTICE: the pre-run missed part of the spectrum
+
+
+def batch_reference(wlg, ctx, req, max_readmit=4, rounds=False):
+    """The four class problems through the batch engine + class probabilities,
+    with the server's re-admission: a class whose pre-run missed part of the
+    spectrum is solved again with twice the pre-run iterations, up to
+    max_readmit times.  rounds=True also returns the number of re-admissions."""
+    out = [None] * len(CLASSES)
+    todo, budget, n_rounds = list(range(len(CLASSES))), req.pre_iterations, 0
+    while todo:
+        probs = []
+        for ci in todo:
+            q = wlg.Problem.from_buffer_copy(req)
+            q.error_class = CLASSES[ci].encode()
+            q.pre_iterations = budget
+            probs.append(q)
+        res = ctx.solve(probs)
+        for ci, r in zip(todo, res):
+            out[ci] = r
+        todo = [ci for ci, r in zip(todo, res) if r[0].status in MISSED]
+        if not todo or n_rounds == max_readmit:
+            break
+        n_rounds += 1
+        budget = min(2 * budget, 1 << 30)
     statuses = [r.status for r, _, _ in out]
     lz = lp = None
     if all(s == 0 for s in statuses):
         lz, lp = (np.asarray(a) for a in wlg.class_log_probs([(E, G) for _, E, G in out], req.prob))
-    return statuses, [r.outer_iterations for r, _, _ in out], lz, lp
+    ret = (statuses, [r.outer_iterations for r, _, _ in out], lz, lp)
+    return ret + (n_rounds,) if rounds else ret
 
 
 def as_tuple(d):
@@ -223,3 +241,34 @@ def test_concurrent_submitters_get_the_sequential_results(cuda):
         assert srv.stats()["completed"] == 12
     for k, rid in got.items():
         assert same(as_tuple(done[rid]), as_tuple(alone[ids[k]])), k
+
+
+def test_missed_spectrum_is_readmitted_with_a_longer_pre_run(cuda):
+    """A 6x6 request whose short pre-run (16 walkers x 200 iterations) misses
+    energies in classes i, v and h: those classes are re-admitted with 400,
+    800, 1600 iterations until their spectrum is complete, class c is kept;
+    every class's result equals the batch engine's at its final pre-run
+    length, bit for bit.  With re-admission off the request retires with
+    WLG_ERR_NEW_ENERGY, as the reference's run would abort."""
+    import qec_pf_wang_landau_gb300 as wlg
+    q = wlg.problem(6, 6, prob=0.1, seed=5, sample=0, pre_walkers=16, pre_intervals=16, pre_iterations=200,
+                    intervals=6, walkers_per_interval=2, beta=0.05, iterations=300, exchange_every=10)
+    ctx = wlg.Context(0)
+    statuses, outer, lz, lp, rounds = batch_reference(wlg, ctx, q, rounds=True)
+    assert statuses == [0, 0, 0, 0] and rounds >= 2
+    first = batch_reference(wlg, ctx, q, max_readmit=0)[0]
+    assert sum(s in MISSED for s in first) >= 2 and 0 in first
+    with wlg.Server(0, epoch_outer=2) as srv:
+        ids = srv.submit([q, q])
+        got = srv.wait(ids, 300)
+        st = srv.stats()
+    for i in ids:
+        d = got[i]
+        assert d.status == 0 and d.readmissions == rounds
+        assert list(d.outer_iterations) == outer
+        assert np.array_equal(np.array(d.log_z), lz) and np.array_equal(np.array(d.log_probs), lp)
+    assert st["readmitted"] == 2 * rounds and st["completed"] == 2
+    with wlg.Server(0, max_readmit=-1) as srv:
+        (i,) = srv.submit([q])
+        d = srv.wait([i], 300)[i]
+    assert d.status == next(s for s in first if s != 0) and d.readmissions == 0
