@@ -41,7 +41,7 @@ BYTES_PER_FLIP = 34  # log g read old + read new + write (24 B), histogram RMW (
 # DRAM bytes (read + write) of one main-run launch of this workload, from an ncu capture of the
 # bench's own launch (dram__bytes_read.sum + dram__bytes_write.sum); walker state never leaves the SM
 MAIN_TRAFFIC_BYTES = 797440
-METRIC = "disorder samples converged/s (6x6 periodic p=0.04, 100 samples x 4 classes)"
+METRIC = "disorder samples converged/s (6x6 pbc p=0.04, 100 samples x 4 classes)"
 CPU_SAMPLE_PROBLEMS = 96
 
 
@@ -759,16 +759,15 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int32+f64",
-        "data": "synthetic: seeded Philox disorder (reference streams)",
-        "config": {"workload": "6x6 periodic p=0.04, 100 samples x ivhc, prerun 128w/32i/1000n, mainrun I=10 W=3 "
-                               "o=0.25 a=0.8 ln f 1e-3 n=1000, exchange every 20",
-                   "problems_per_gpu": len(probs), "l2": "flushed between steps",
+        "data": "synthetic, seeded Philox",
+        "config": {"workload": "6x6 pbc p.04 100x4cls pre128/32/1000 I10 W3 o.25 a.8 lnf1e-3 n1000 c20",
+                   "l2": "flushed",
                    "teams_per_cta": {f"f{t['form']}/t{t['team']}": t["per_cta"] for t in tuning}},
         "e2e": {"value": converged / t_e2e, "unit": "samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": MAIN_TRAFFIC_BYTES,
-                     "peak_kind": peak_kind, "basis": f"{BYTES_PER_FLIP} B/flip"},
+                     "peak_kind": peak_kind},
         "flips_per_s": flips / t_main,
     }
     if clocks is not None:
@@ -777,19 +776,24 @@ def run_ours(args):
         return r4(line)
     cpu_pps, cpu_fps, cpu_s = cpu_run(CPU_SAMPLE_PROBLEMS, os.cpu_count() or 1)
     line["cpu_baseline"] = {"value": cpu_pps, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"{CPU_SAMPLE_PROBLEMS} problems (samples 0-23 x ivhc), {cpu_s:.1f} s"}
+                            "sample": f"{CPU_SAMPLE_PROBLEMS} problems"}
     # comparison arms on the same 400 problems (samples/s, converged; device or wall time as stated)
     plain_pps, plain_s, plain_launches = plain_run()
     ref_cuda = reference_cuda_run()
     x0_pps, x0_out = engine_x0_run(ctx, 3)
-    arms = {"plain": plain_pps, "engine_x0": x0_pps}
+    # arms (samples/s): plain form, this engine without exchange (x0, the
+    # reference's behaviour at -c 20), the reference's kernels (ref); ratios
+    arms = {"plain": plain_pps, "x0": x0_pps}
     if ref_cuda is not None:
-        arms["reference_cuda"] = ref_cuda[0]
-        arms["x0_over_reference_cuda"] = x0_pps / ref_cuda[0]
-    arms["value_over_plain"] = value / plain_pps
+        arms["ref"] = ref_cuda[0]
+        arms["x0/ref"] = x0_pps / ref_cuda[0]
+    arms["v/plain"] = value / plain_pps
     line["arms"] = arms
-    line["accuracy"] = accuracy({"engine": last_out, "engine_x0": x0_out},
-                                ref_cuda[2] if ref_cuda is not None else None)
+    acc = accuracy({"engine": last_out, "engine_x0": x0_out}, ref_cuda[2] if ref_cuda is not None else None)
+    short = {"engine": "eng", "engine_x0": "x0", "reference_cuda": "ref"}
+    line["accuracy"] = {"rms": {short[k]: v for k, v in acc["rms"].items()},
+                        "cls_ok": {short[k]: v for k, v in acc["class_decisions_equal_exact"].items()},
+                        "of": acc["samples"], "sets_ok": acc["engine_sets_exact"]}
     sec = secondary_ceilings(achieved, flips / t_main)
     detail = {"plain": {"seconds": plain_s, "kernel_launches": plain_launches,
                         "what": "same 400 problems, reference structure on this engine's operator kernels"},
@@ -798,8 +802,8 @@ def run_ours(args):
                                                   "prerun/mainrun order; no exchange at -c 20 (its counter never "
                                                   "advances)"},
               "engine_x0": "this engine, exchange_mode 0 (the reference's behaviour at -c 20), device time",
-              **sec}
-    line["roofline_smem_frac"] = sec["roofline_smem"]["frac"]
+              "accuracy": acc, **sec}
+    line["roofline"]["smem_frac"] = sec["roofline_smem"]["frac"]
     if not args.no_extra:
         legs = {"batched": batched_run(), "large": large_run(), "large_converged": large_converged_run(),
                 "serving": serving_run()}
@@ -810,27 +814,28 @@ def run_ours(args):
 
 
 def legs_summary(legs):
-    """A few numbers per extra leg for the headline line."""
+    """A few numbers per extra leg for the headline line: samples/s, times in
+    ms, flip rates in G/s; x0 = this engine without exchange, ref = the
+    reference's kernels."""
     out = {}
     b = legs.get("batched")
     if b:
-        out["batched"] = {"value": b["value"], "ok": b["status_counts"].get("0", 0),
-                          "rms": {k: v["rms_mean"] for k, v in b["accuracy"].items()}}
-        for k in ("critical_path_ms", "main_ms", "arms"):
-            if k in b:
-                out["batched"][k] = b[k]
+        out["batched"] = {"v": b["value"], "ok": b["status_counts"].get("0", 0),
+                          "rms": max(v["rms_mean"] for v in b["accuracy"].values()) if b["accuracy"] else None,
+                          "crit": b.get("critical_path_ms"), "main": b.get("main_ms")}
     g = legs.get("large")
     if g:
-        out["large"] = {k: v["flips_per_s"] for k, v in g.items() if isinstance(v, dict)}
+        out["large_gf"] = [v["flips_per_s"] / 1e9 for v in g.values() if isinstance(v, dict)]
     c = legs.get("large_converged")
     if c:
-        out["large_converged"] = {k: c[k]["value"] for k in ("engine", "engine_x0", "plain", "reference_cuda")
-                                  if k in c}
-        out["large_converged"]["rms_vs_ref"] = {k: c[k].get("rms_vs_reference") for k in ("engine", "engine_x0")}
+        out["lconv"] = {"v": c["engine"]["value"], "x0": c["engine_x0"]["value"], "plain": c["plain"]["value"]}
+        if "reference_cuda" in c:
+            out["lconv"]["ref"] = c["reference_cuda"]["value"]
+            out["lconv"]["rms_ref"] = c["engine"].get("rms_vs_reference")
     v = legs.get("serving")
     if v:
-        out["serving"] = {"ok": v["retired_ok"], "of": v["requests"], "readmitted": v["requests_readmitted"],
-                          "p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"]}
+        out["serving"] = {"ok": v["retired_ok"], "of": v["requests"], "readm": v["requests_readmitted"],
+                          "p50": v["p50_ms"], "p99": v["p99_ms"]}
     return out
 
 

@@ -20,6 +20,7 @@ namespace wlg {
 // ---- kernels (wlg_engine.cu)
 wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem, int8_t* Jpool, uint8_t* seen_pool,
                             int8_t* found_pool, int* fflag_pool, cudaStream_t s);
+// variant: kernel_variant (form | kKernelRows)
 int main_batch_capacity(int variant, int cta_threads, int smem);
 wlg_status launch_main_batch(int variant, const MainDesc* d_descs, const int* d_order, int n, int team_size,
                              int team_bytes, int teams_per_cta, int grid, int* d_next, double* gpool,
@@ -190,5 +191,10 @@ inline int fit_form(const MainDesc& d, int team)
   const int form = main_form(d);
   return form == 0 && team_bytes(d, 0, team) > kSmemBytes ? 3 : form;
 }
+
+// The kernel of a main-run launch: its form (fit_form, 0-3) plus
+// kKernelRows when its problems keep lattices one row per word
+// (lattice_rows; forms 0 and 3 only).  Problems of one launch share both.
+inline int kernel_variant(const MainDesc& d, int team) { return fit_form(d, team) | (d.rows != 0 ? kKernelRows : 0); }
 
 }  // namespace wlg

@@ -301,12 +301,15 @@ __device__ __forceinline__ int energy_after_flip(const Lat& l, uint64_t JR, uint
 // arithmetic as wl.cu:52-156: with r, ru, rd the rows of the site and of the
 // rows above and below, a bond is unsatisfied (s_a s_b J = -1) exactly when
 // the two spin bits and the coupling bit have odd parity, and flipping the
-// site changes the energy by 2 (deg - 2 unsat) over its deg bonds (4, or
-// fewer on an open edge, wl.cu:134-137).  Also returns the offset of the
-// site's row word and that word with the site flipped.
+// site changes the energy by 2 (deg - 2 unsat) over its deg bonds.  Without
+// a branch on the boundary: a horizontal bond belongs to the column on its
+// left and is missing on an open lattice exactly when that is the last
+// column (hedge clears its bit), a vertical bond is missing at the first or
+// last row (wl.cu:134-137).  Also returns the offset of the site's row word
+// and that word with the site flipped.
 __device__ __forceinline__ int energy_after_flip_rows(const Lat& l, const uint32_t* Jr_s, const uint32_t* Jd_s,
-                                                      int site, int E, const MainDesc& d, int& row_off,
-                                                      uint32_t& row_new)
+                                                      int site, int E, const MainDesc& d, uint32_t hedge, bool open,
+                                                      int& row_off, uint32_t& row_new)
 {
   const int i = static_cast<int>((static_cast<uint32_t>(site) * d.site_magic) >> 20);
   const int j = site - i * d.Y;
@@ -318,18 +321,13 @@ __device__ __forceinline__ int energy_after_flip_rows(const Lat& l, const uint32
   const uint32_t mjl = j == 0 ? 1u << (d.Y - 1) : mj >> 1;
   const uint32_t rr = (r >> 1) | ((r & 1u) << (d.Y - 1));  // bit c: spin (i, c + 1 mod Y)
   const uint32_t h = r ^ rr ^ Jr_s[i];                     // bit c: bond (i, c)-(i, c + 1) unsatisfied
-  const uint32_t vu = (r ^ ru ^ Jd_s[iu]) & mj;            // bond (i - 1, j)-(i, j) unsatisfied
-  const uint32_t vd = (r ^ rd ^ Jd_s[i]) & mj;             // bond (i, j)-(i + 1, j) unsatisfied
+  const bool up = !open || i != 0, dn = !open || i != d.X - 1;
+  const uint32_t vu = up ? (r ^ ru ^ Jd_s[iu]) & mj : 0u;  // bond (i - 1, j)-(i, j) unsatisfied
+  const uint32_t vd = dn ? (r ^ rd ^ Jd_s[i]) & mj : 0u;   // bond (i, j)-(i + 1, j) unsatisfied
+  const uint32_t hm = (mj | mjl) & hedge;
   row_new = r ^ mj;
-  int unsat, deg;
-  if (d.boundary == 0) {
-    unsat = __popc(h & (mj | mjl)) + __popc(vu) + __popc(vd);
-    deg = 4;
-  } else {
-    const uint32_t hm = (j < d.Y - 1 ? mj : 0u) | (j > 0 ? mjl : 0u);
-    unsat = __popc(h & hm) + (i > 0 ? __popc(vu) : 0) + (i < d.X - 1 ? __popc(vd) : 0);
-    deg = __popc(hm) + (i > 0 ? 1 : 0) + (i < d.X - 1 ? 1 : 0);
-  }
+  const int unsat = __popc(h & hm) + __popc(vu) + __popc(vd);
+  const int deg = __popc(hm) + (up ? 1 : 0) + (dn ? 1 : 0);
   return E + 2 * (deg - 2 * unsat);
 }
 
@@ -351,7 +349,7 @@ __device__ __forceinline__ long long device_clock_ns()
   return t;
 }
 
-template <bool kReg, bool kTable, bool kGlobalG>
+template <bool kReg, bool kTable, bool kGlobalG, bool kRows>
 __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, unsigned char* base, double* gslot,
                             const uint32_t* __restrict__ Jpool, const uint32_t* __restrict__ latpool,
                             const int* __restrict__ winpool, const uint32_t* __restrict__ maskpool,
@@ -474,6 +472,9 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   const int lo = live ? w_start[b] : 0, hi = live ? w_end[b] : 0, bb = live ? w_base[b] : 0;
   const int step_mask = (1 << d.lg) - 1;
   const int span = d.e_max - d.e_min;
+  // row layout: open lattices have no bond right of the last column
+  const bool open_bc = d.boundary != 0;
+  const uint32_t hedge = open_bc ? ~(1u << (d.Y - 1)) : 0xFFFFFFFFu;
   const int Lm1 = d.L - 1;
 
   long long outer = 0;
@@ -597,12 +598,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
           const int deg = __popcll(nt.x);
           const int sb = static_cast<int>((lt.r >> site) & 1ull);
           En = E + 2 * (1 - 2 * sb) * (deg - 2 * unsat);
-        } else if constexpr (!kReg) {
-          if (d.rows != 0) {
-            En = energy_after_flip_rows(lt, Jr_s, Jd_s, site, E, d, row_off, row_new);
-          } else {
-            En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
-          }
+        } else if constexpr (kRows) {
+          En = energy_after_flip_rows(lt, Jr_s, Jd_s, site, E, d, hedge, open_bc, row_off, row_new);
         } else {
           En = energy_after_flip<kReg>(lt, JR, JD, Jr_s, Jd_s, site, E, d);
         }
@@ -640,12 +637,8 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
         }
         const bool commit = act && !need_site && !need_acc && !bad;
         const bool acc = commit && inside && (ovr_acc >= 0 ? ovr_acc != 0 : fast_acc);
-        if constexpr (!kReg) {
-          if (d.rows != 0) {
-            if (acc) lt.s[row_off] = row_new;
-          } else {
-            flip_spin<kReg>(lt, site, acc);
-          }
+        if constexpr (kRows) {
+          if (acc) lt.s[row_off] = row_new;
         } else {
           flip_spin<kReg>(lt, site, acc);
         }
@@ -888,7 +881,7 @@ __device__ void run_problem(const MainDesc& d, int p, const Team& team, int t, u
   team.sync();
 }
 
-template <bool kReg, bool kTable, bool kGlobalG, int kMaxThreads>
+template <bool kReg, bool kTable, bool kGlobalG, bool kRows, int kMaxThreads>
 __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __restrict__ descs, const int* __restrict__ order,
                                                      int n, int team_size, int team_bytes, int* __restrict__ next,
                                                      double* __restrict__ gpool, long long gslot_doubles,
@@ -916,8 +909,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_main_batch(const MainDesc* __re
     if (d.off_state >= 0 && results[p].done != 0) continue;  // resumable run that finished in an earlier launch
     double* gslot = kGlobalG ? gpool + (static_cast<long long>(blockIdx.x) * (blockDim.x / team_size) + tix) * gslot_doubles
                              : nullptr;
-    run_problem<kReg, kTable, kGlobalG>(d, p, team, t, base, gslot, Jpool, latpool, winpool, maskpool, outpool, results,
-                                        statepool);
+    run_problem<kReg, kTable, kGlobalG, kRows>(d, p, team, t, base, gslot, Jpool, latpool, winpool, maskpool, outpool,
+                                               results, statepool);
   }
 }
 
@@ -940,17 +933,21 @@ wlg_status launch_pre_batch(const PreDesc* d_descs, int n, int threads, int smem
 using MainFn = void (*)(const MainDesc*, const int*, int, int, int, int*, double*, long long, const uint32_t*,
                         const uint32_t*, const int*, const uint32_t*, double*, MainResult*, unsigned char*);
 
-// variant: 0 = spins and log g in shared memory, 1 = spins in a register,
-// 2 = register spins + neighbour table, 3 = spins in shared memory, FP64 log g
-// in a global pool (problems too large for one SM's shared memory)
+// variant (kernel_variant): form 0 = spins and log g in shared memory,
+// 1 = spins in a register, 2 = register spins + neighbour table, 3 = spins
+// in shared memory, FP64 log g in a global pool (problems too large for one
+// SM's shared memory); plus kKernelRows (4) for lattices one row per word
+// (forms 0 and 3)
 template <int kMaxThreads>
 MainFn main_fn_for(int variant)
 {
   switch (variant) {
-    case 1: return &k_main_batch<true, false, false, kMaxThreads>;
-    case 2: return &k_main_batch<true, true, false, kMaxThreads>;
-    case 3: return &k_main_batch<false, false, true, kMaxThreads>;
-    default: return &k_main_batch<false, false, false, kMaxThreads>;
+    case 1: return &k_main_batch<true, false, false, false, kMaxThreads>;
+    case 2: return &k_main_batch<true, true, false, false, kMaxThreads>;
+    case 3: return &k_main_batch<false, false, true, false, kMaxThreads>;
+    case 0 | kKernelRows: return &k_main_batch<false, false, false, true, kMaxThreads>;
+    case 3 | kKernelRows: return &k_main_batch<false, false, true, true, kMaxThreads>;
+    default: return &k_main_batch<false, false, false, false, kMaxThreads>;
   }
 }
 

@@ -46,6 +46,8 @@ struct PreDesc {
 // -1 coupling; right bonds (site, site + 1 in the row) and down bonds (site,
 // site + Y) are packed the same way as the sites that own them.
 WLG_HD inline bool lattice_rows(int X, int Y) { return X * Y > 64 && Y >= 2 && Y <= 32; }
+// bit of a main-run kernel variant (kernel_variant) for the row layout
+constexpr int kKernelRows = 4;
 WLG_HD inline int lattice_words(int X, int Y) { return lattice_rows(X, Y) ? X : (X * Y + 31) / 32; }
 // word and bit of site q (q = i*Y + j)
 WLG_HD inline void lattice_bit(int X, int Y, int q, int& word, int& bit)

@@ -736,7 +736,7 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ex.device);
   // one launch per (form, team size); the form by lattice storage (fit_form)
   std::map<std::pair<int, int>, std::vector<int>> groups;
-  for (int i = 0; i < m; ++i) groups[{wlg::fit_form(prep.main[i], prep.main[i].team), prep.main[i].team}].push_back(i);
+  for (int i = 0; i < m; ++i) groups[{wlg::kernel_variant(prep.main[i], prep.main[i].team), prep.main[i].team}].push_back(i);
   // Longest problems first (larger lattices take more outer iterations of
   // longer steps): the groups' launches are issued, and each group's queue
   // is ordered, by decreasing lattice size, so the batch's longest serial
@@ -757,7 +757,7 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
     int bytes = 0;
     int Lmax = 1;
     for (int i : idx) {
-      bytes = std::max(bytes, wlg::team_bytes(prep.main[i], variant, team));
+      bytes = std::max(bytes, wlg::team_bytes(prep.main[i], variant & 3, team));
       Lmax = std::max(Lmax, prep.main[i].L);
     }
     if (bytes > wlg::kSmemBytes) return fail(ex, WLG_ERR_INVALID, "problem state exceeds shared memory");
@@ -813,7 +813,7 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
     const int cap = wlg::main_batch_capacity(variant, team * per_cta, bytes * per_cta);
     if (cap <= 0) return fail(ex, WLG_ERR_CUDA, "main-run configuration does not fit an SM");
     grids[g] = std::min(cap, (count + per_cta - 1) / per_cta);
-    if (variant == 3) {
+    if ((variant & 3) == 3) {
       gpool_off[g] = gpool_doubles;
       gpool_doubles += static_cast<long long>(grids[g]) * per_cta * Lmax * team;
     }
@@ -835,7 +835,7 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
     for (size_t g = 0; g < launches.size() && s2 == WLG_OK; ++g) {
       const auto [variant, team, bytes, per_cta, first, count, Lmax] = launches[g];
       const int grid = grids[g];
-      double* gp = variant == 3 ? static_cast<double*>(d_gpool) + gpool_off[g] : nullptr;
+      double* gp = (variant & 3) == 3 ? static_cast<double*>(d_gpool) + gpool_off[g] : nullptr;
       s2 = wlg::launch_main_batch(
         variant, static_cast<const MainDesc*>(d_md), static_cast<const int*>(d_order) + first, count, team, bytes,
         per_cta, grid, static_cast<int*>(d_next) + g, gp, static_cast<long long>(Lmax) * team,
@@ -844,7 +844,7 @@ wlg_status run_main(Exec& ex, wlg_result* results, Prepared& prep, const Handoff
         static_cast<unsigned char*>(d_state), n_fork > 0 ? ex.aux[g % n_fork] : ex.stream);
       if (s2 == WLG_OK) {
         ++ex.launches;
-        ex.main_forms |= 1 << variant;
+        ex.main_forms |= 1 << (variant & 3);
       }
     }
     for (int a = 0; a < n_fork; ++a) {  // join (also after a failed launch)
@@ -1312,7 +1312,7 @@ wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, i
     std::map<std::pair<int, int>, std::vector<int>> groups;
     for (size_t i = 0; i < prep.main.size(); ++i) {
       const MainDesc& d = prep.main[i];
-      groups[{fit_form(d, d.team), d.team}].push_back(static_cast<int>(i));
+      groups[{kernel_variant(d, d.team), d.team}].push_back(static_cast<int>(i));
     }
     std::map<std::pair<int, int>, int> best;
     std::vector<wlg_tuning> found;
@@ -1323,7 +1323,7 @@ wlg_status wlg_context_autotune(wlg_context* ctx, const wlg_problem* problems, i
         sub.main_problem.push_back(prep.main_problem[i]);
       }
       const int limit = key.second <= 256 ? 256 / key.second : 1;
-      wlg_tuning t{key.first, key.second, 1, 0.0f, 0};
+      wlg_tuning t{key.first & 3, key.second, 1, 0.0f, 0};
       float best_ms = 0.0f;
       for (int c = 1; c <= limit; c *= 2) {
         const std::map<std::pair<int, int>, int> force{{key, c}};

@@ -628,8 +628,8 @@ void wlg_server::finish_admission(AdmitJob& aj)
     }
     MainDesc d = prep.main[main_of[k]];
     const BlockLayout bl = block_layout(d.team, d.I, d.L, d.nwL, d.nwM);
-    const int form = fit_form(d, d.team);
-    if (team_bytes(d, form, d.team) > kSmemLimit || bl.bytes > bb.bytes) {
+    const int form = kernel_variant(d, d.team);  // form | kKernelRows
+    if (team_bytes(d, form & 3, d.team) > kSmemLimit || bl.bytes > bb.bytes) {
       arena.release(boff, bb.bytes);
       class_done(id, cls, WLG_ERR_INVALID, 0, {});
       continue;
@@ -715,7 +715,7 @@ bool wlg_server::launch()
     if (static_cast<int>(g.waited.size()) < static_cast<int>(admit_ev.size())) g.waited.resize(admit_ev.size(), 0);
     for (int s : g.members) {
       const Problem& pr = probs[s];
-      bytes = std::max(bytes, team_bytes(pr.d, g.form, g.team));
+      bytes = std::max(bytes, team_bytes(pr.d, g.form & 3, g.team));
       if (!g.waited[pr.ready_ev]) {
         if (!cuda_ok(cudaStreamWaitEvent(g.stream, admit_ev[pr.ready_ev], 0))) {
           fail_all("stream wait");

@@ -106,3 +106,35 @@ def test_batched_accuracy_scores_every_side_against_exact():
         assert a["curves"] == min(2 if L <= 10 else 1, bench.BATCHED_ACCURACY_PER_SIDE[L])
         assert a["energy_sets_exact"]
         assert a["rms_mean"] < 1e-12 and a["max_abs"] < 1e-12
+
+
+def test_headline_line_fits_the_kept_tail():
+    """The headline line, with every key at a worst-case width, stays within
+    the last 1500 characters of output that a run's record keeps (newline
+    included)."""
+    import json
+    import bench
+    legs = {"batched": {"value": 97.71234, "status_counts": {"0": 1990, "3": 10}, "critical_path_ms": 17920.123,
+                        "main_ms": 19850.456, "accuracy": {f"{L}x{L}": {"rms_mean": 0.0712345} for L in (4, 6, 8, 10, 12)}},
+            "large": {"workload": "w", "16x16": {"flips_per_s": 80480000000.0}, "24x24": {"flips_per_s": 6.785e10}},
+            "large_converged": {k: {"value": 0.2047123, "rms_vs_reference": 0.1193456}
+                                for k in ("engine", "engine_x0", "plain", "reference_cuda")},
+            "serving": {"retired_ok": 165, "requests": 165, "requests_readmitted": 20, "p50_ms": 5023.123,
+                        "p99_ms": 63920.123}}
+    line = {"metric": bench.METRIC, "value": 6065.123, "unit": "samples/s", "n_gpus": 1, "steps": 20, "warmup": 5,
+            "ms_per_step": 65.95123, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32+f64", "data": "synthetic, seeded Philox",
+            "config": {"workload": "6x6 pbc p.04 100x4cls pre128/32/1000 I10 W3 o.25 a.8 lnf1e-3 n1000 c20",
+                       "l2": "flushed", "teams_per_cta": {"f2/t32": 4}},
+            "e2e": {"value": 5927.123, "unit": "samples/s", "h2d_bytes_per_step": 237140, "d2h_bytes_per_step": 1000880},
+            "gpu_launches": 100, "roofline": {"bound": "hbm", "achieved": 529.123, "peak": 6677.0, "unit": "GB/s",
+                                              "frac": 0.0792512, "traffic": 797440, "peak_kind": "measured",
+                                              "smem_frac": 0.01319123},
+            "flips_per_s": 15560000000.0, "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"]},
+            "cpu_baseline": {"value": 182.5123, "unit": "samples/s", "cores": 72, "kind": "port",
+                             "sample": "96 problems"},
+            "arms": {"plain": 237.4123, "x0": 7105.123, "ref": 138.4123, "x0/ref": 51.33123, "v/plain": 25.54123},
+            "accuracy": {"rms": {"eng": 0.17871, "x0": 0.1841, "ref": 0.1731},
+                         "cls_ok": {"eng": 100, "x0": 99, "ref": 98}, "of": 100, "sets_ok": True},
+            "legs": bench.legs_summary(legs)}
+    assert len(json.dumps(bench.r4(line))) + 1 <= 1490

@@ -1,7 +1,8 @@
-"""The C++ examples of INTEGRATION.md compile against include/wlg.h: the
-integration guide cannot drift from the header (argument counts, types and
-order, struct field order in the aggregate initialisers).  CPU only
-(syntax check, nothing runs)."""
+"""The C++ examples of the maintainers' integration guide (at the repository
+root) compile against include/wlg.h, so the guide cannot drift from the
+header (argument counts, types and order, struct field order in the
+aggregate initialisers); its Python example names only what the binding
+has.  CPU only (syntax check, nothing runs)."""
 import os
 import re
 import shutil
@@ -10,6 +11,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GUIDE = os.path.join(ROOT, "INTEGRATION.md")
 
 # Names the examples take from the surrounding caller code (the reference's
 # mainrun.cu buffers and options, a caller's lattice and request variables).
@@ -38,7 +40,7 @@ LOCALS = """
 
 
 def cpp_blocks():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(GUIDE).read()
     return re.findall(r"```cpp\n(.*?)```", text, re.S)
 
 
@@ -69,7 +71,7 @@ def test_python_example_names_exist():
     methods it calls exist on Context and Server."""
     import ast
     import qec_pf_wang_landau_gb300 as wlg
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(GUIDE).read()
     (block,) = re.findall(r"```python\n(.*?)```", text, re.S)
     tree = ast.parse(block)
     for node in ast.walk(tree):
