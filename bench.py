@@ -217,7 +217,7 @@ def accuracy(arms, ref_runs):
 
 
 SERVING = dict(rate=200.0, seconds=1.0, side_min=4, side_max=16, prob_min=0.02, prob_max=0.12, beta=1e-6,
-               walkers_per_interval=4, wait_s=120.0, seed=2026)
+               walkers_per_interval=4, wait_s=240.0, seed=2026)
 
 
 def serving_requests(n_max: int = 100000):
@@ -516,7 +516,7 @@ def c3_arms_run(per_group=None, sides=None, ref_budget_s=600.0):
     return res
 
 
-LARGE_CONV = dict(side=16, samples=1, classes="v", prob=0.10, seed=4343, beta=1e-5)
+LARGE_CONV = dict(side=16, samples=1, classes="ivhc", prob=0.10, seed=4343, beta=1e-4)
 
 
 def large_converged_run(side=None, samples=None, beta=None, classes=None):
