@@ -78,7 +78,6 @@ struct MainDesc {
   double site_scale;             // (N - 1) + 0.999999, wl.cu:64
   long long max_outer;           // 0 = no cap
   int nwL;                       // 32-bit words per lattice (lattice_words)
-  int rows;                      // 1: one row per word (lattice_rows)
   int nwM;                       // 32-bit words of the compact spectrum mask
   long long off_J;               // words: right bonds [nwL], down bonds [nwL]
   long long off_lat;             // words: start lattice of each window [I][nwL]
@@ -87,6 +86,7 @@ struct MainDesc {
   long long off_out;             // doubles: [I][L] walker-0 log g (compact)
   long long off_state;           // bytes: saved state (state_layout) of a resumable run, -1 = run to the end
   int epoch_outer;               // resumable runs: outer iterations per launch before the state is saved
+  int rows;                      // 1: one row per word (lattice_rows)
 };
 
 // Per-problem result of the main run (of one launch, for resumable runs).
