@@ -72,10 +72,19 @@ PrerunOut run_prerun(int X, int Y, int boundary, float prob, char cls, int seed,
   std::vector<int> hs(static_cast<size_t>(n_int)), he(static_cast<size_t>(n_int));
   long long tot = 0;
   int len_int = 0;
-  orc_interval_results(e_min, e_max, static_cast<unsigned>(n_int), 1, 1.0F, hs.data(), he.data(), &tot, &len_int);
+  const int irc =
+    orc_interval_results(e_min, e_max, static_cast<unsigned>(n_int), 1, 1.0F, hs.data(), he.data(), &tot, &len_int);
 
   const size_t total_walker = static_cast<size_t>(R) * walkers;
   PrerunOut out;
+  if (irc != 0) {  // prerun.cu:23-35: interval_results throws (empty coarse bins); nothing runs
+    out.J.assign(static_cast<size_t>(R) * 2 * N, 0);
+    out.seen.assign(static_cast<size_t>(R) * (4 * N + 1), 0);
+    out.found_flag.assign(static_cast<size_t>(R) * n_int, 0);
+    out.found_lat.assign(static_cast<size_t>(R) * n_int * N, 0);
+    out.found_energy.assign(static_cast<size_t>(R) * n_int, 0);
+    return out;
+  }
   out.J.assign(static_cast<size_t>(R) * 2 * N, 0);
   orc_init_interactions(out.J.data(), static_cast<size_t>(N), R, seed, prob);
   orc_apply_error_class(out.J.data(), X, Y, R, cls);

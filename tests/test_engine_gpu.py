@@ -482,3 +482,27 @@ def test_mainrun_entry_refuses_values_other_than_pm1(cuda, what):
     st = wlg.lib().wlg_mainrun(ctx._h, C.cast(probs, C.c_void_p), 1, O.ptr(seen), O.ptr(J), O.ptr(found),
                                O.ptr(energy), O.ptr(lat), 60.0, C.cast(res, C.c_void_p), O.ptr(E), O.ptr(G), len(E))
     assert st == 1 and "problem 0 not +-1" in wlg.lib().wlg_context_last_error(ctx._h).decode()
+
+
+def test_main_times_bound_the_main_run(cuda):
+    """wlg_last_main_times: every problem that ran its main run has
+    0 <= start <= end on the device clock, the first start is 0 and the last
+    end lies within the main run's event-timed duration; a problem refused at
+    the hand-off (no stored lattice for a window) reports -1."""
+    import qec_pf_wang_landau_gb300 as wlg
+    refused = wlg.problem(6, 6, prob=0.08, seed=100, sample=3, pre_walkers=16, pre_intervals=16, pre_iterations=300,
+                          intervals=14, walkers_per_interval=2, overlap=0.8)
+    ok = [wlg.problem(X, X, boundary=b, seed=7, sample=k, beta=0.01, iterations=400)
+          for k, (X, b) in enumerate([(4, 0), (6, 1), (5, 0), (8, 0)])]
+    probs = ok[:2] + [refused] + ok[2:]
+    ctx = wlg.Context(0)
+    out = ctx.solve(probs)
+    t0, t1 = ctx.main_times()
+    assert len(t0) == len(probs)
+    assert out[2][0].status == 5 and t0[2] == -1 and t1[2] == -1  # WLG_ERR_NO_LATTICE
+    ran = [i for i in range(len(probs)) if i != 2]
+    assert all(out[i][0].status == 0 for i in ran)
+    assert all(0 <= t0[i] <= t1[i] for i in ran)
+    assert min(t0[i] for i in ran) == 0.0
+    main_ms = ctx.stats()["main_ms"]
+    assert max(t1[i] for i in ran) <= main_ms * 1.01 + 0.05
