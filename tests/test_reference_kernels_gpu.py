@@ -475,3 +475,46 @@ def test_full_main_run_equals_reference_kernels(cuda, ref):
             assert np.array_equal(s, out["start"][k * I:(k + 1) * I]) and np.array_equal(e, out["end"][k * I:(k + 1) * I])
             for b in range(I):
                 assert np.array_equal(wins[b], out["windows"][k * I + b]), (cls, k, b)
+
+
+@pytest.mark.parametrize("X,Y,boundary,cls", [(6, 6, 0, "c"), (5, 6, 1, "h")])
+def test_batched_exchange_every_iteration_equals_reference_kernels(cuda, ref, X, Y, boundary, cls):
+    """The reference's main loop at -c 1 exchanges every outer iteration
+    (its counter stays 1, mainrun.cu:241, :346).  From the same pre-run, its
+    kernels and this engine's persistent batched main run (exchange mode 0,
+    every iteration, the reference's global parity) give equal walker-0 log g
+    in every window after 25 outer iterations, bit for bit; ln f never reaches
+    its final value in that span (2^-25 > 1e-9), so no window finishes and the
+    reference's finished-window walk (Q5) is not entered; two walkers per window
+    keep its averaging order-free.  Without exchange the result differs."""
+    import qec_pf_wang_landau_gb300 as wlg
+    seed, R, pre_w, pre_i, pre_n, I, W, cap = 4321, 3, 64, 16, 4000, 8, 2, 25
+    N = X * Y
+    pre = prerun_outputs(X, Y, boundary, 0.1, cls, seed, R, pre_w, pre_i, pre_n)
+    for k in range(R):
+        cnt = O.exact_counts(pre["J"][k * 2 * N:(k + 1) * 2 * N], X, Y, boundary)
+        assert np.array_equal(pre["seen"][k * (4 * N + 1):(k + 1) * (4 * N + 1)] != 0, cnt != 0)
+    lat = pre["found_lat"].copy()
+    for q in range(R * pre_i):
+        if not pre["found_flag"][q]:
+            lat[q * N:(q + 1) * N] = 0
+    out = O.reference_mainrun(X, Y, boundary, seed, R, pre_i, pre["seen"], pre["J"], lat, pre["found_energy"], I, W,
+                              0.3, 0.8, 1e-9, 500, 1, max_outer=cap)
+    assert out["status"] == 3 and out["outer"] == cap
+
+    def mine(xc):
+        probs = [wlg.problem(X, Y, boundary=boundary, prob=0.1, error_class=cls, seed=seed, sample=k,
+                             pre_walkers=pre_w, pre_intervals=pre_i, pre_iterations=pre_n, intervals=I,
+                             walkers_per_interval=W, overlap=0.3, beta=1e-9, iterations=500, exchange_every=xc,
+                             exchange_mode=0, global_parity=1, max_outer=cap) for k in range(R)]
+        return wlg.Context(0).solve_raw(probs)
+    with_x, without_x = mine(1), mine(2)
+    differs = False
+    for k in range(R):
+        r, s, e, wins = with_x[k]
+        assert r.status == 7 and r.outer_iterations == cap  # WLG_ERR_TIMEOUT at the cap
+        assert np.array_equal(s, out["start"][k * I:(k + 1) * I]) and np.array_equal(e, out["end"][k * I:(k + 1) * I])
+        for b in range(I):
+            assert np.array_equal(wins[b], out["windows"][k * I + b]), (k, b)
+            differs |= not np.array_equal(without_x[k][3][b], wins[b])
+    assert differs
