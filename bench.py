@@ -12,9 +12,17 @@ value  = converged problems / (pre-run kernel + host hand-off + main-run
          kernel time), the kernels timed with CUDA events;
 e2e    = the same through wlg_solve() with host buffers: problem
          descriptors in, stitched log g out, everything in the timed region;
+arms   = the same 400 problems through the plain form, this engine without
+         exchange (the reference's behaviour at -c 20) and the reference's own
+         CUDA kernels (oracle/ref_harness.cu), untimed by the contract;
+legs   = the heterogeneous batched, large-lattice, converged large-lattice
+         and serving workloads (summaries; full details on the line printed
+         just before the headline, prefixed "detail ").
 --impl reference times the CPU restatement of the reference's path (the
 reference has no CPU implementation and its CUDA build needs Boost/HDF5) on
-all host cores.
+all host cores, the same 400 problems per step.
+--leg NAME runs one leg alone (c3_arms: the heterogeneous workload against the
+plain form and the reference's kernels, ~20 minutes).
 
 Multi-GPU (torchrun): the problems shard by disorder sample, one shard of
 400 problems per rank (weak scaling), no collective on the data path.
