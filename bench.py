@@ -590,6 +590,55 @@ def large_converged_run(side=None, samples=None, beta=None, classes=None):
     return res
 
 
+def large_saturated_run(sides=(16, 24), samples=152, caps=(10, 40)):
+    """Throughput of the large-lattice workload with the GPU full: `samples`
+    disorder samples (152: one 512-thread team per SM for this engine; 152 x 64
+    blocks for the reference's kernels), class v, p = 0.10, 64 windows x 8
+    walkers, overlap 0.3, no exchange in every arm (the reference's behaviour
+    at -c 10), each run capped at caps[0] and then caps[1] outer iterations
+    (ln f 1e-8 is never reached, so no sample finishes).  The difference of
+    the two runs' times over the difference of the caps is the time of one
+    outer iteration of all samples, pre-run and set-up cancelled: with the
+    same algorithm the iterations to convergence are the same in every arm,
+    so its ratio between arms is their throughput ratio."""
+    import qec_pf_wang_landau_gb300 as wlg
+    import oracle as O
+    res = {"workload": f"{samples} samples x class v, p=0.10, I=64 W=8 o=0.3, no exchange, outer capped at {caps}"}
+    for L in sides:
+        N = L * L
+
+        def probs(cap):
+            return [wlg.problem(L, L, prob=0.10, error_class="v", seed=5151, sample=k, pre_walkers=128,
+                                pre_intervals=128, pre_iterations=1000 * N, intervals=64, walkers_per_interval=8,
+                                overlap=0.3, alpha=0.8, beta=1e-8, iterations=1000, exchange_every=10,
+                                exchange_mode=0, max_outer=cap) for k in range(samples)]
+        ctx = wlg.Context(0)
+        eng, pl, rf = [], [], []
+        for cap in caps:
+            out = ctx.solve_raw(probs(cap))
+            eng.append((ctx.stats()["main_ms"], max(r.outer_iterations for r, _, _, _ in out)))
+            t0 = time.perf_counter()
+            outp, _ = wlg.solve_plain(probs(cap))
+            pl.append((1e3 * (time.perf_counter() - t0), max(r.outer_iterations for r, _, _ in outp)))
+            if O.reference_harness() is not None:
+                o = O.reference_run(L, L, 0, 0.10, "v", 5151, samples, 128, 128, 1000 * N, 64, 8, 0.3, 0.8, 1e-8, 1000,
+                                    10, max_outer=cap, want_raw=False)
+                rf.append((o["main_ms"], o["outer"]))
+
+        def per_outer(v):
+            return (v[1][0] - v[0][0]) / max(v[1][1] - v[0][1], 1)
+        r = {"engine_ms_per_outer": per_outer(eng), "plain_ms_per_outer": per_outer(pl),
+             "outer": [eng[0][1], eng[1][1]]}
+        if rf:
+            r["reference_ms_per_outer"] = per_outer(rf)
+            r["reference_over_engine"] = r["reference_ms_per_outer"] / r["engine_ms_per_outer"]
+            r["reference_outer"] = [rf[0][1], rf[1][1]]
+        r["plain_over_engine"] = r["plain_ms_per_outer"] / r["engine_ms_per_outer"]
+        res[f"{L}x{L}"] = r
+        print("partial " + json.dumps(r4({f"{L}x{L}": r})), flush=True)
+    return res
+
+
 LARGE = dict(sides=(16, 24), samples=38, prob=0.10, seed=4242, max_outer=10)
 
 
@@ -945,7 +994,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--profile-case", default=None, help="run a small fixed case for a profiler and exit")
-    ap.add_argument("--leg", default=None, choices=["serving", "batched", "large", "c3_arms", "large_converged", "peaks"],
+    ap.add_argument("--leg", default=None,
+                    choices=["serving", "batched", "large", "c3_arms", "large_converged", "large_saturated", "peaks"],
                     help="run one extra leg alone and print it")
     ap.add_argument("--per-group", type=int, default=None, help="c3_arms: samples per group")
     ap.add_argument("--sides", type=int, nargs="*", default=None, help="c3_arms: lattice sides")
@@ -964,6 +1014,7 @@ def main():
         legs = {"serving": serving_run, "batched": batched_run, "large": large_run,
                 "c3_arms": lambda: c3_arms_run(args.per_group, args.sides),
                 "large_converged": lambda: large_converged_run(args.side, args.samples, args.beta, args.classes),
+                "large_saturated": large_saturated_run,
                 "peaks": lambda: wlg.measure_peaks(0)}
         print(json.dumps(r4({args.leg: legs[args.leg]()})), flush=True)
         return
