@@ -15,9 +15,11 @@ e2e    = the same through wlg_solve() with host buffers: problem
 arms   = the same 400 problems through the plain form, this engine without
          exchange (the reference's behaviour at -c 20) and the reference's own
          CUDA kernels (oracle/ref_harness.cu), untimed by the contract;
-legs   = the heterogeneous batched, large-lattice, converged large-lattice
-         and serving workloads (summaries; full details on the line printed
-         just before the headline, prefixed "detail ").
+legs   = the heterogeneous batched, large-lattice, saturated large-lattice
+         (152 samples, time per outer iteration against the plain form and
+         the reference's kernels), converged large-lattice and serving
+         workloads (summaries; full details on the line printed just before
+         the headline, prefixed "detail ").
 --impl reference times the CPU restatement of the reference's path (the
 reference has no CPU implementation and its CUDA build needs Boost/HDF5) on
 all host cores, the same 400 problems per step.
@@ -864,8 +866,8 @@ def run_ours(args):
               "accuracy": acc, **sec}
     line["roofline"]["smem_frac"] = sec["roofline_smem"]["frac"]
     if not args.no_extra:
-        legs = {"batched": batched_run(), "large": large_run(), "large_converged": large_converged_run(),
-                "serving": serving_run()}
+        legs = {"batched": batched_run(), "large": large_run(), "large_saturated": large_saturated_run(),
+                "large_converged": large_converged_run(), "serving": serving_run()}
         detail.update(legs)
         line["legs"] = legs_summary(legs)
     print("detail " + json.dumps(r4(detail)), flush=True)
@@ -874,27 +876,35 @@ def run_ours(args):
 
 def legs_summary(legs):
     """A few numbers per extra leg for the headline line: samples/s, times in
-    ms, flip rates in G/s; x0 = this engine without exchange, ref = the
-    reference's kernels."""
+    s, flip rates in G/s (gflips, per lattice side); x0 = this engine without
+    exchange, ref = the reference's kernels; batched crit = critical path /
+    main-run time; lconv rms = the engine's log g RMS against ref."""
     out = {}
     b = legs.get("batched")
     if b:
+        crit, main = b.get("critical_path_ms"), b.get("main_ms")
         out["batched"] = {"v": b["value"], "ok": b["status_counts"].get("0", 0),
                           "rms": max(v["rms_mean"] for v in b["accuracy"].values()) if b["accuracy"] else None,
-                          "crit": b.get("critical_path_ms"), "main": b.get("main_ms")}
+                          "main_s": main / 1e3 if main else None,
+                          "crit": crit / main if crit and main else None}
     g = legs.get("large")
     if g:
-        out["large_gf"] = [v["flips_per_s"] / 1e9 for v in g.values() if isinstance(v, dict)]
+        out["gflips"] = [v["flips_per_s"] / 1e9 for v in g.values() if isinstance(v, dict)]
+    t = legs.get("large_saturated")
+    if t:
+        # per side, time per outer iteration with the GPU full, no exchange: [reference / engine, plain / engine]
+        out["sat"] = [[v.get("reference_over_engine"), v["plain_over_engine"]] for v in t.values()
+                      if isinstance(v, dict)]
     c = legs.get("large_converged")
     if c:
-        out["lconv"] = {"v": c["engine"]["value"], "x0": c["engine_x0"]["value"], "plain": c["plain"]["value"]}
+        out["lconv"] = {"v": c["engine"]["value"], "x0": c["engine_x0"]["value"]}
         if "reference_cuda" in c:
             out["lconv"]["ref"] = c["reference_cuda"]["value"]
-            out["lconv"]["rms_ref"] = c["engine"].get("rms_vs_reference")
+            out["lconv"]["rms"] = c["engine"].get("rms_vs_reference")
     v = legs.get("serving")
     if v:
-        out["serving"] = {"ok": v["retired_ok"], "of": v["requests"], "readm": v["requests_readmitted"],
-                          "p50": v["p50_ms"], "p99": v["p99_ms"]}
+        out["serving"] = {"ok": f'{v["retired_ok"]}/{v["requests"]}', "readm": v["requests_readmitted"],
+                          "p99_s": v["p99_ms"] / 1e3}
     return out
 
 

@@ -117,6 +117,8 @@ def test_headline_line_fits_the_kept_tail():
     legs = {"batched": {"value": 97.71234, "status_counts": {"0": 1990, "3": 10}, "critical_path_ms": 17920.123,
                         "main_ms": 19850.456, "accuracy": {f"{L}x{L}": {"rms_mean": 0.0712345} for L in (4, 6, 8, 10, 12)}},
             "large": {"workload": "w", "16x16": {"flips_per_s": 80480000000.0}, "24x24": {"flips_per_s": 6.785e10}},
+            "large_saturated": {"workload": "w", "16x16": {"reference_over_engine": 60.59123, "plain_over_engine": 4.12123},
+                                "24x24": {"reference_over_engine": 46.77123, "plain_over_engine": 3.60823}},
             "large_converged": {k: {"value": 0.2047123, "rms_vs_reference": 0.1193456}
                                 for k in ("engine", "engine_x0", "plain", "reference_cuda")},
             "serving": {"retired_ok": 165, "requests": 165, "requests_readmitted": 20, "p50_ms": 5023.123,
