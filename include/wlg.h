@@ -290,8 +290,8 @@ wlg_status wlg_solve_raw(wlg_context* ctx, const wlg_problem* problems, int n, w
  * caller left them (400 problems of 6x6 lattices fit).  Runs on the current
  * device and `stream`; the call synchronises `stream` itself (after the
  * pre-run and at the end) and returns once the stream has finished the
- * batch.  The first call on a device looks up the arena's device address,
- * so make that first call before any stream capture.  All calls share the
+ * batch.  The first call on a device also looks up the arena's device
+ * address.  All calls share the
  * arena, which keeps the last call's contents: calls that overlap on the
  * GPU race, so serialise them. */
 wlg_status wlg_solve_raw_noalloc(const wlg_problem* problems, int n, wlg_result* results, int* win_start,
