@@ -275,6 +275,11 @@ def serving_run():
         st = srv.stats()
     done = [got[i] for i in ids if i in got]
     lat = np.array([d.done_ms - d.submit_ms for d in done]) if done else np.zeros(1)
+    side = {i: q.X for i, q in zip(ids, reqs)}
+    slow = []  # the longest requests: what their latency is made of
+    for d in sorted(done, key=lambda d: d.submit_ms - d.done_ms)[:3]:
+        slow.append({"latency_s": (d.done_ms - d.submit_ms) / 1e3, "side": side[int(d.id)],
+                     "outer_ivhc": list(d.outer_iterations), "readmissions": d.readmissions, "status": d.status})
     span_s = (max(d.done_ms for d in done) - min(d.submit_ms for d in done)) / 1e3 if done else float("nan")
     statuses = {}
     for d in done:
@@ -285,7 +290,7 @@ def serving_run():
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "throughput_req_s": len(done) / span_s if done else 0.0,
             "epochs": st["epochs"], "prerun_launches": st["prerun_launches"], "readmitted": st["readmitted"],
-            "requests_readmitted": sum(1 for d in done if d.readmissions > 0),
+            "requests_readmitted": sum(1 for d in done if d.readmissions > 0), "slowest": slow,
             "note": f"requests not retired within {SERVING['wait_s']:.0f} s are left out of the percentiles"}
 
 

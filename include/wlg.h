@@ -448,7 +448,7 @@ typedef struct {
 typedef struct {
   unsigned long long id;       /* as returned by wlg_server_submit */
   int status;                  /* WLG_OK, or the first failing class's status */
-  int readmissions;            /* times some of its classes were re-admitted (max_readmit) */
+  int readmissions;            /* the most re-admissions of any one of its classes (max_readmit) */
   long long outer_iterations[4]; /* main-run outer iterations per class i, v, h, c */
   double log_z[4];             /* log Z_c at beta_N = ln((1-p)/p) / 2 */
   double log_probs[4];         /* log Z_c - logsumexp_c log Z_c */
@@ -458,7 +458,7 @@ typedef struct {
 typedef struct {
   long long submitted, completed, resident_problems, epochs, main_launches, prerun_launches;
   long long bytes_in_use, bytes_budget;
-  long long readmitted;        /* re-admissions (of one or more classes of a request) */
+  long long readmitted;        /* class re-admissions */
 } wlg_server_stats;
 
 wlg_status wlg_server_create(int device, const wlg_server_config* config, wlg_server** out);

@@ -201,9 +201,9 @@ struct Request {
   wlg_problem q{};
   std::vector<int8_t> J;  // given class-'i' couplings (2N), empty: drawn
   wlg_decoded out{};
-  int remaining = kClasses;
+  int remaining = kClasses;              // classes not yet done
   unsigned todo = (1u << kClasses) - 1;  // classes of the next admission
-  unsigned retry = 0;                    // classes to re-admit once every class of this admission is done
+  bool part = false;                     // a pending re-admission of one class of an active request
   int pre_iterations[kClasses] = {};     // per class; 0: q.pre_iterations
   int attempts[kClasses] = {};           // re-admissions so far, per class
   int status[kClasses] = {};
@@ -386,12 +386,16 @@ void wlg_server::fail_all(const std::string& why)
     finished.push_back(r.out);
     ++stats.completed;
   };
+  // a re-admitted class's entry (part) belongs to a request in `active`,
+  // which retires once
   for (auto& [id, r] : active) retire_failed(r);
   active.clear();
-  for (auto& [id, r] : pending) retire_failed(r);
+  for (auto& [id, r] : pending)
+    if (!r.part) retire_failed(r);
   pending.clear();
   if (job) {  // an admission in flight: its thread reads only the job's copies of the parameters
-    for (auto& [id, r] : job->batch) retire_failed(r);
+    for (auto& [id, r] : job->batch)
+      if (!r.part) retire_failed(r);
     job->batch.clear();
   }
   cv_out.notify_all();
@@ -443,33 +447,31 @@ void wlg_server::class_done(unsigned long long id, int cls, int status, long lon
   r.out.outer_iterations[cls] = outer;
   r.curve[cls] = std::move(curve);
   // A class whose pre-run missed part of the spectrum (a walker later found a
-  // new energy, or a window got no start lattice) is re-admitted with twice
-  // the pre-run iterations: a deterministic function of the request, so the
+  // new energy, or a window got no start lattice) is re-admitted at once, on
+  // its own, with twice the pre-run iterations, while the request's other
+  // classes keep running: a deterministic function of the request, so the
   // result equals the batch engine's for that larger pre-run.  (The
   // reference aborts the whole run instead.)
-  if ((status == WLG_ERR_NEW_ENERGY || status == WLG_ERR_NO_LATTICE) && r.attempts[cls] < cfg.max_readmit)
-    r.retry |= 1u << cls;
-  if (--r.remaining > 0) return;
-  if (r.retry != 0) {
-    for (int c = 0; c < kClasses; ++c)
-      if ((r.retry >> c) & 1u) {
-        r.pre_iterations[c] = std::min(2 * static_cast<long long>(r.pre_iter(c)), 1ll << 30);
-        r.attempts[c] += 1;
-        r.status[c] = WLG_OK;
-        r.curve[c].clear();
-      }
-    r.todo = r.retry;
-    r.remaining = std::popcount(r.retry);
-    r.retry = 0;
-    r.out.readmissions += 1;
+  if ((status == WLG_ERR_NEW_ENERGY || status == WLG_ERR_NO_LATTICE) && r.attempts[cls] < cfg.max_readmit) {
+    r.pre_iterations[cls] = static_cast<int>(std::min(2 * static_cast<long long>(r.pre_iter(cls)), 1ll << 30));
+    r.attempts[cls] += 1;
+    r.status[cls] = WLG_OK;
+    r.curve[cls].clear();
+    r.out.readmissions = std::max(r.out.readmissions, r.attempts[cls]);
     {
       std::lock_guard<std::mutex> lk(mu);
       ++stats.readmitted;
     }
-    pending.emplace_front(id, std::move(r));
-    active.erase(it);
-    return;
+    Request c;  // what the admission reads: parameters, couplings, this class's pre-run length
+    c.q = r.q;
+    c.J = r.J;
+    c.todo = 1u << cls;
+    c.part = true;
+    std::copy(r.pre_iterations, r.pre_iterations + kClasses, c.pre_iterations);
+    pending.emplace_front(id, std::move(c));
+    return;  // the class stays outstanding in r.remaining
   }
+  if (--r.remaining > 0) return;
   complete(id, r);
   active.erase(it);
 }
@@ -600,11 +602,13 @@ void wlg_server::finish_admission(AdmitJob& aj)
   }
   if (st != WLG_OK) {
     for (size_t k = 0; k < block_off.size(); ++k) arena.release(block_off[k], bound[k].bytes);
-    for (auto& [id, r] : batch) active.emplace(id, std::move(r));
+    for (auto& [id, r] : batch)
+      if (!r.part) active.emplace(id, std::move(r));
     fail_all("pre-run: " + aj.err);
     return;
   }
-  for (auto& [id, r] : batch) active.emplace(id, std::move(r));
+  for (auto& [id, r] : batch)
+    if (!r.part) active.emplace(id, std::move(r));
   // which batch problems reach the main run
   std::vector<int> main_of(static_cast<size_t>(n), -1);
   for (size_t i = 0; i < prep.main.size(); ++i) main_of[prep.main_problem[i]] = static_cast<int>(i);
