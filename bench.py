@@ -358,14 +358,19 @@ def critical_path(ctx, probs, out):
     for _, d in ev:
         live += d
         peak = max(peak, live)
-    by_side = {}
-    for p, sp, ok in zip(probs, span, ran):
+    by_side, start_by_side = {}, {}
+    for p, sp, a, ok in zip(probs, span, t0, ran):
         if ok:
             by_side.setdefault(f"{p.X}x{p.Y}", []).append(sp)
+            start_by_side.setdefault(f"{p.X}x{p.Y}", []).append(a)
+    z = int(np.argmax(np.where(ran, t1, -1.0)))  # the problem that ends the main run
     return {"critical_path_ms": float(span[q]),
             "critical_problem": {"side": probs[q].X, "boundary": probs[q].boundary, "windows": probs[q].intervals,
-                                 "outer_iterations": int(r.outer_iterations),
+                                 "outer_iterations": int(r.outer_iterations), "start_ms": float(t0[q]),
                                  "us_per_outer": 1e3 * float(span[q]) / max(int(r.outer_iterations), 1)},
+            "last_problem": {"side": probs[z].X, "start_ms": float(t0[z]), "span_ms": float(span[z]),
+                             "outer_iterations": int(out[z][0].outer_iterations)},
+            "start_ms_max_by_side": {k: float(max(v)) for k, v in sorted(start_by_side.items())},
             "last_end_ms": float(t1[ran].max()),
             "end_ms_p50_p90": [float(np.percentile(t1[ran], 50)), float(np.percentile(t1[ran], 90))],
             "span_ms_max_by_side": {k: float(max(v)) for k, v in sorted(by_side.items())},
