@@ -979,8 +979,10 @@ def profile_case(name: str):
     """Small fixed cases for ncu captures (not bench numbers): `main6x6` = 152
     problems of the workload (samples 0-37 x ivhc, one per SM) capped at 20
     outer iterations; `large16` = the large-lattice leg's 152 16x16 problems
-    (512-thread teams) capped at 3 outer iterations.  Each is solved twice
-    (capture the second main-run launch)."""
+    (512-thread teams) capped at 3 outer iterations; `batched` = the
+    heterogeneous batched leg's 2000 problems capped at 3 outer iterations
+    (three main-run launches side by side: 12x12, 10x10, and 4x4-8x8 teams).
+    Each is solved twice (capture the second solve's main-run launches)."""
     import qec_pf_wang_landau_gb300 as wlg
     wlg.build()
     if name == "main6x6":
@@ -993,6 +995,9 @@ def profile_case(name: str):
                              overlap=0.3, alpha=0.8, beta=1e-8, iterations=1000, exchange_every=10)
                  for k in range(c["samples"]) for cl in "ivhc"]
         cap = 3
+    elif name == "batched":
+        probs = batched_problems()
+        cap = 3
     else:
         raise SystemExit(f"unknown profile case {name}")
     for p in probs:
@@ -1001,8 +1006,7 @@ def profile_case(name: str):
     for _ in range(2):
         out = ctx.solve_raw(probs)
     st = ctx.stats()
-    walkers = probs[0].intervals * probs[0].walkers_per_interval
-    steps = sum(r.flips for r, _, _, _ in out) / walkers
+    steps = sum(r.flips / (p.intervals * p.walkers_per_interval) for p, (r, _, _, _) in zip(probs, out))
     print(json.dumps({"case": name, "main_ms": st["main_ms"], "main_forms": st["main_forms"],
                       "walker_steps_per_problem": steps / len(probs)}))
 
