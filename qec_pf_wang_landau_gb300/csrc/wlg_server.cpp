@@ -22,7 +22,9 @@
 //   retire  - when an epoch's event completes, its snapshot of the result
 //             table says which problems finished; their walker-0 log g is
 //             copied back and stitched, and a request whose four classes are
-//             done gets its class log-probabilities;
+//             done gets its class log-probabilities; a class whose pre-run
+//             missed part of the spectrum goes back to admit at once, alone,
+//             with a longer pre-run;
 //   reclaim - a finished problem's block and slot are reused once no
 //             in-flight epoch lists it any more.
 //
