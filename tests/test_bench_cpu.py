@@ -140,3 +140,25 @@ def test_headline_line_fits_the_kept_tail():
                          "cls_ok": {"eng": 100, "x0": 99, "ref": 98}, "of": 100, "sets_ok": True},
             "legs": bench.legs_summary(legs)}
     assert len(json.dumps(bench.r4(line))) + 1 <= 1490
+
+
+def test_critical_path_names_the_longest_chain_and_the_last_problem():
+    """critical_path on made-up main-run times: the longest span, the problem
+    that ends last (a late starter with a shorter span), the latest start per
+    side, the most problems running at once; problems without a main run
+    (start -1) are left out."""
+    import types
+    import bench
+
+    class Ctx:
+        def main_times(self):
+            return (np.array([0.0, 0.0, 3000.0, -1.0, 100.0]), np.array([9000.0, 2000.0, 11000.0, -1.0, 600.0]))
+
+    probs = [types.SimpleNamespace(X=x, Y=x, boundary=0, intervals=8) for x in (12, 10, 10, 8, 12)]
+    out = [(types.SimpleNamespace(outer_iterations=n),) for n in (900, 200, 700, 0, 50)]
+    cp = bench.critical_path(Ctx(), probs, out)
+    assert cp["critical_path_ms"] == 9000.0 and cp["critical_problem"]["side"] == 12
+    assert cp["critical_problem"]["outer_iterations"] == 900 and cp["critical_problem"]["us_per_outer"] == 1e4
+    assert cp["last_problem"] == {"side": 10, "start_ms": 3000.0, "span_ms": 8000.0, "outer_iterations": 700}
+    assert cp["start_ms_max_by_side"] == {"10x10": 3000.0, "12x12": 100.0}
+    assert cp["last_end_ms"] == 11000.0 and cp["concurrent_peak"] == 3
