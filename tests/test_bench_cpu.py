@@ -162,3 +162,18 @@ def test_critical_path_names_the_longest_chain_and_the_last_problem():
     assert cp["last_problem"] == {"side": 10, "start_ms": 3000.0, "span_ms": 8000.0, "outer_iterations": 700}
     assert cp["start_ms_max_by_side"] == {"10x10": 3000.0, "12x12": 100.0}
     assert cp["last_end_ms"] == 11000.0 and cp["concurrent_peak"] == 3
+
+
+def test_a_failing_leg_is_reported_not_raised():
+    import bench
+
+    def broken():
+        raise RuntimeError("no device")
+    legs = {"batched": bench.run_leg(broken), "serving": {"retired_ok": 3, "requests": 3, "requests_readmitted": 0,
+                                                        "p99_ms": 1500.0}}
+    assert legs["batched"] == {"error": "RuntimeError: no device"}
+    import time
+    late = bench.run_leg(lambda: {"value": 1.0}, time.perf_counter() - bench.LEG_BUDGET_S - 1)
+    assert late["error"].startswith("skipped")
+    assert bench.run_leg(lambda: {"value": 1.0}, time.perf_counter()) == {"value": 1.0}
+    assert bench.legs_summary(legs) == {"failed": ["batched"], "serving": {"ok": "3/3", "readm": 0, "p99_s": 1.5}}
