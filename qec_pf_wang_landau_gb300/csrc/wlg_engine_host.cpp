@@ -1454,15 +1454,17 @@ struct ArenaExec final : Exec {
 // alone (windows of the full range [-2N, 2N], energy step 2), so oversized
 // batches are rejected before anything runs.  This includes the global log g
 // pool of the form-3 launches (run_main): one slice of L x team doubles per
-// resident team, at most (problems + teams per CTA - 1) slices per team size,
-// counted for every problem whose full-range state would not fit shared
-// memory (its real windows are never wider, so no form-3 problem is missed).
+// resident team, at most (problems + teams per CTA - 1) slices per launch (one
+// launch per team size and lattice layout), counted for every problem whose
+// full-range state would not fit shared memory (its real windows are never
+// wider, so no form-3 problem is missed).
 size_t noalloc_bound(const wlg_problem* probs, int n)
 {
   auto pad = [](size_t x) { return (x + 255) & ~size_t{255}; };
   size_t pre_desc = 0, j8 = 0, seen = 0, found = 0, fflag = 0;
   size_t md = 0, order = 0, jw = 0, latw = 0, win = 0, mask = 0, out = 0, res = 0;
-  std::map<int, std::pair<size_t, size_t>> pool;  // team size -> (form-3 problems, largest L)
+  // (team size, row layout) -> (form-3 problems, largest L): run_main's form-3 launches
+  std::map<std::pair<int, bool>, std::pair<size_t, size_t>> pool;
   for (int p = 0; p < n; ++p) {
     const wlg_problem& q = probs[p];
     const size_t N = static_cast<size_t>(q.X) * q.Y, I = static_cast<size_t>(q.intervals);
@@ -1477,7 +1479,7 @@ size_t noalloc_bound(const wlg_problem* probs, int n)
     d.nwM = static_cast<int>((nbins + 31) / 32);
     const int team = wlg::round32(q.intervals * q.walkers_per_interval);
     if (wlg::fit_form(d, team) == 3) {
-      auto& e = pool[team];
+      auto& e = pool[{team, wlg::lattice_rows(q.X, q.Y)}];
       e.first += 1;
       e.second = std::max(e.second, nbins);
     }
@@ -1496,7 +1498,8 @@ size_t noalloc_bound(const wlg_problem* probs, int n)
     res += sizeof(MainResult);
   }
   size_t gpool = 0;
-  for (const auto& [team, e] : pool) {
+  for (const auto& [key, e] : pool) {
+    const int team = key.first;
     const size_t per_cta_max = team <= 256 ? static_cast<size_t>(256 / team) : 1;
     gpool += (e.first + per_cta_max - 1) * e.second * static_cast<size_t>(team) * sizeof(double);
   }
